@@ -1,0 +1,180 @@
+/*
+ * pgeof_cuda.h -- C ABI of libpgeof_cuda.so, the GB300 (sm_103a) implementation
+ * of pgeof's neighbour-search and local-PCA geometric-feature path.
+ *
+ * Plain pointers, sizes and status codes only. Every entry point replaces one
+ * function of pgeof 0.3.3 (drprojects/point_geometric_features); the citation
+ * above each declaration names the reference function it stands in for, with
+ * the same argument meaning, output layout and error conditions.
+ *
+ * Two families:
+ *   pgeof_*       device pointers (inputs and outputs already in GPU memory),
+ *                 enqueued on `stream`, asynchronous. Host-side argument errors
+ *                 are returned immediately; errors that only the data reveals
+ *                 (an `nn` index >= n_xyz, a decreasing `nn_ptr`) are recorded
+ *                 on the device and reported by pgeof_take_device_errors().
+ *   pgeof_host_*  host pointers, synchronous: the reference's own contract
+ *                 (host arrays in, host arrays out). Copies run inside the call
+ *                 and data errors come back as the return code.
+ *
+ * Conventions shared with the reference:
+ *   xyz / data / query : float32 (n, 3) row-major (RefCloud<float>, pca.hpp:18)
+ *   nn, nn_ptr         : uint32 CSR; neighbours of point i are
+ *                        nn[nn_ptr[i] : nn_ptr[i+1]]; n_points = len(nn_ptr) - 1
+ *   features           : float32 row-major, EFeatureID order (pca.hpp:47-63)
+ *   eigenvalues        : in Eigen's ascending order, exactly as pca.hpp:79-97
+ *                        uses them (val[0] = smallest); see pgeof_set_eig_order.
+ *   normal sign        : v2 flipped so that v2.z >= 0 (pca.hpp:96)
+ */
+#ifndef PGEOF_CUDA_H
+#define PGEOF_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGEOF_ABI_VERSION 1
+
+/* Return codes. INVALID_ARGUMENT and DATA_ERROR are the reference's
+ * std::invalid_argument (nanobind maps it to ValueError). */
+typedef enum pgeof_status {
+    PGEOF_OK = 0,
+    PGEOF_ERR_INVALID_ARGUMENT = 1, /* bad size / parameter (reference throws)          */
+    PGEOF_ERR_DATA = 2,             /* nn index >= n_xyz, nn_ptr decreasing or > len(nn) */
+    PGEOF_ERR_OUT_OF_MEMORY = 3,
+    PGEOF_ERR_CUDA = 4,             /* CUDA runtime failure (message has the detail)      */
+    PGEOF_ERR_NO_DEVICE = 5,        /* no usable GB300 / CUDA device                       */
+    PGEOF_ERR_INTERNAL = 6          /* an internal bound was exceeded                      */
+} pgeof_status;
+
+/* EFeatureID, include/pca.hpp:47-63 (same integer values). */
+typedef enum pgeof_feature_id {
+    PGEOF_LINEARITY = 0,
+    PGEOF_PLANARITY = 1,
+    PGEOF_SCATTERING = 2,
+    PGEOF_VERTICALITY_PGEOF = 3,
+    PGEOF_NORMAL_X = 4,
+    PGEOF_NORMAL_Y = 5,
+    PGEOF_NORMAL_Z = 6,
+    PGEOF_LENGTH = 7,
+    PGEOF_SURFACE = 8,
+    PGEOF_VOLUME = 9,
+    PGEOF_CURVATURE = 10,
+    PGEOF_K_OPTIMAL = 11,
+    PGEOF_VERTICALITY = 12,
+    PGEOF_EIGENTROPY = 13
+} pgeof_feature_id;
+
+/* A cudaStream_t. NULL is the legacy default stream. */
+typedef void* pgeof_stream_t;
+
+/* ---------------------------------------------------------------- library */
+int pgeof_abi_version(void);
+const char* pgeof_status_string(int status);
+/* Detail of the last failure on the calling host thread (never NULL). */
+const char* pgeof_last_error_message(void);
+/* Number of kernels this library has launched in this process. */
+uint64_t pgeof_kernel_launch_count(void);
+/* Eigenpair order fed to the feature formulas: 0 = ascending (Eigen's order,
+ * what pca.hpp:79-97 does, the default), 1 = descending (val[0] = largest, so
+ * v2 is the surface normal). Process-wide. */
+int pgeof_set_eig_order(int order);
+int pgeof_get_eig_order(void);
+/* Synchronises `stream` and returns (then clears) the device-side data-error
+ * bits recorded since the last call (bit 0: nn index out of range, bit 1:
+ * nn_ptr not monotone or beyond len(nn), bit 2: internal bound exceeded). */
+int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits);
+
+/* ------------------------------------------------ device-pointer API (async) */
+
+/* nanoflann_knn_search<float>, include/nn_search.hpp:31-67.
+ * For each query row: the `knn` nearest data rows (self included when the query
+ * is in the data), ascending squared distance; ties ordered by lower index.
+ * indices / sqr_dist: (n_query, knn). Errors: knn > n_data. */
+int pgeof_knn_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query, uint32_t knn,
+                         uint32_t* indices, float* sqr_dist, pgeof_stream_t stream);
+
+/* nanoflann_radius_search<float>, include/nn_search.hpp:85-132.
+ * Up to max_knn nearest data rows with squared distance < search_radius^2
+ * (computed in float), ascending. Missing entries: index -1, distance 0, except
+ * that a row with fewer than max_knn hits reports search_radius^2 in its last
+ * distance slot (nanoflann's RKNNResultSet::init). Errors: max_knn > n_data. */
+int pgeof_radius_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                            float search_radius, uint32_t max_knn, int32_t* indices, float* sqr_dist,
+                            pgeof_stream_t stream);
+
+/* compute_geometric_features<float, 11>, include/pgeof.hpp:75-117.
+ * features: (n_points, 11); rows with fewer than k_min neighbours are 0.
+ * Errors: k_min < 1. */
+int pgeof_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                               const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features,
+                               pgeof_stream_t stream);
+
+/* compute_geometric_features_multiscale<float, 11>, include/pgeof.hpp:123-211.
+ * k_scales is a HOST array; features: (n_points, n_scales, 11). A point stops
+ * at the first scale larger than its neighbour count (later scales are 0).
+ * Errors: a scale < 1 or scales not non-decreasing (check_scales, :123-132). */
+int pgeof_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                          const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                          int64_t n_scales, float* features, pgeof_stream_t stream);
+
+/* compute_geometric_features_optimal<float, 12>, include/pgeof.hpp:243-310.
+ * features: (n_points, 12); column 11 holds the optimal k as a float.
+ * Errors: k_min < 1 and k_min_search < 1; k_step == 0 (the reference divides
+ * by it). */
+int pgeof_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                       const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
+                                       uint32_t k_min_search, float* features, pgeof_stream_t stream);
+
+/* compute_geometric_features_selected<float>, include/pgeof.hpp:325-375.
+ * Radius search (< search_radius^2) around every point, the nearest max_knn
+ * kept, PCA, then the selected EFeatureIDs in list order. `selected` is a HOST
+ * array of EFeatureID values. Points with fewer than 2 points inside the radius
+ * are 0; K_optimal and unknown ids stay 0. features: (n, n_selected). */
+int pgeof_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
+                                        const int32_t* selected, int64_t n_selected, float* features,
+                                        pgeof_stream_t stream);
+
+/* compute_geometric_features_selected<double>, include/pgeof.hpp:325-375
+ * (bound first in src/pgeof_ext.cpp:148). Same as above in double precision. */
+int pgeof_compute_features_selected_f64(const double* xyz, int64_t n, double search_radius, uint32_t max_knn,
+                                        const int32_t* selected, int64_t n_selected, double* features,
+                                        pgeof_stream_t stream);
+
+/* ------------------------------------------------ host-pointer API (sync) */
+/* Same semantics as the device entry points above; every pointer is host
+ * memory. These are what the Python drop-in binding calls for numpy inputs. */
+
+/* include/nn_search.hpp:31-67 */
+int pgeof_host_knn_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                              uint32_t knn, uint32_t* indices, float* sqr_dist);
+/* include/nn_search.hpp:85-132 */
+int pgeof_host_radius_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                                 float search_radius, uint32_t max_knn, int32_t* indices, float* sqr_dist);
+/* include/pgeof.hpp:75-117 */
+int pgeof_host_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                    const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features);
+/* include/pgeof.hpp:123-211 */
+int pgeof_host_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                               const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                               int64_t n_scales, float* features);
+/* include/pgeof.hpp:243-310 */
+int pgeof_host_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                            const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min,
+                                            uint32_t k_step, uint32_t k_min_search, float* features);
+/* include/pgeof.hpp:325-375 (float) */
+int pgeof_host_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
+                                             const int32_t* selected, int64_t n_selected, float* features);
+/* include/pgeof.hpp:325-375 (double) */
+int pgeof_host_compute_features_selected_f64(const double* xyz, int64_t n, double search_radius,
+                                             uint32_t max_knn, const int32_t* selected, int64_t n_selected,
+                                             double* features);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PGEOF_CUDA_H */

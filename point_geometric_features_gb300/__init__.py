@@ -1,0 +1,218 @@
+"""GB300 (sm_103a) implementation of pgeof's neighbour search and local-PCA
+geometric features, with pgeof's Python API.
+
+Drop-in for ``pgeof`` (src/pgeof/__init__.py:1-9): the same names, argument
+names, defaults and numpy dtype rules. Every call runs on the GPU through
+``libpgeof_cuda.so``; there is no CPU fallback -- if the native library is
+missing, importing this package raises ImportError.
+
+Besides numpy arrays, every function also accepts ``torch.cuda`` tensors: the
+work then stays on the device (inputs are read in place, outputs are CUDA
+tensors, the call is enqueued on the current torch stream).
+"""
+
+from __future__ import annotations
+
+import os as _os
+import sys as _sys
+
+try:
+    from . import pgeof_ext as _ext
+except ImportError as _e:  # no CPU fallback: fail loudly
+    raise ImportError(
+        "point_geometric_features_gb300: the native library is not built "
+        f"({_e}). Build it with `python point_geometric_features_gb300/_build.py` "
+        "(needs nvcc for sm_103a)."
+    ) from _e
+
+from .pgeof_ext import EFeatureID  # noqa: E402
+
+# enum values exported at module level like pgeof_ext's export_values()
+for _name, _val in EFeatureID.__members__.items():
+    globals()[_name] = _val
+
+LIBRARY_PATH = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "libpgeof_cuda.so")
+
+__all__ = [
+    "EFeatureID",
+    "compute_features",
+    "compute_features_multiscale",
+    "compute_features_optimal",
+    "knn_search",
+    "radius_search",
+    "compute_features_selected",
+    "set_eig_order",
+    "get_eig_order",
+    "kernel_launch_count",
+    "check_device_errors",
+]
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch") and hasattr(x, "is_cuda")
+
+
+def set_eig_order(order: str) -> None:
+    """Eigenpair order fed to the feature formulas.
+
+    ``"ascending"`` (default) is what pgeof 0.3.3 does: include/pca.hpp:79-97
+    uses Eigen's eigenvalues unsorted, i.e. ascending. ``"descending"`` puts the
+    largest eigenvalue first, which makes Normal_x/y/z the surface normal.
+    """
+    _ext._set_eig_order({"ascending": 0, "descending": 1}[order])
+
+
+def get_eig_order() -> str:
+    return ("ascending", "descending")[_ext._get_eig_order()]
+
+
+def kernel_launch_count() -> int:
+    """Number of CUDA kernels libpgeof_cuda has launched in this process."""
+    return int(_ext._launch_count())
+
+
+def check_device_errors(stream=None) -> None:
+    """Synchronise ``stream`` (torch stream, int handle or None = current torch
+    stream) and raise ValueError if a device call saw invalid CSR input."""
+    bits = _ext._take_device_errors(_stream_handle(stream))
+    if bits & 1:
+        raise ValueError("nn holds an index >= the number of points in xyz")
+    if bits & 2:
+        raise ValueError("nn_ptr must be non-decreasing and its values must not exceed len(nn)")
+    if bits & 4:
+        raise RuntimeError("neighbour selection exceeded its refinement bound")
+
+
+def _stream_handle(stream=None) -> int:
+    if isinstance(stream, int):
+        return stream
+    torch = _sys.modules.get("torch")
+    if stream is None:
+        if torch is None or not torch.cuda.is_available():
+            return 0
+        return int(torch.cuda.current_stream().cuda_stream)
+    return int(stream.cuda_stream)
+
+
+# --------------------------------------------------------------- device path
+def _dev_cloud(t, name, dtype_name="float32"):
+    torch = _sys.modules["torch"]
+    want = getattr(torch, dtype_name)
+    if not t.is_cuda or t.dtype != want or t.dim() != 2 or t.shape[1] != 3 or not t.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous CUDA {dtype_name} tensor of shape (n, 3)")
+    return t
+
+
+def _dev_index(t, name):
+    torch = _sys.modules["torch"]
+    ok_dtypes = (torch.int32,) + ((torch.uint32,) if hasattr(torch, "uint32") else ())
+    if not t.is_cuda or t.dtype not in ok_dtypes or t.dim() != 1 or not t.is_contiguous():
+        raise TypeError(f"{name} must be a contiguous 1-D CUDA uint32 (or int32) tensor")
+    return t
+
+
+def _uint32_empty(torch, shape, device):
+    if hasattr(torch, "uint32"):
+        return torch.empty(shape, dtype=torch.uint32, device=device)
+    return torch.empty(shape, dtype=torch.int32, device=device)
+
+
+def _finish(check, stream):
+    if check:
+        check_device_errors(stream)
+
+
+def _dev_features(kind, xyz, nn, nn_ptr, args, check):
+    torch = _sys.modules["torch"]
+    _dev_cloud(xyz, "xyz")
+    _dev_index(nn, "nn")
+    _dev_index(nn_ptr, "nn_ptr")
+    n = nn_ptr.shape[0] - 1
+    with torch.cuda.device(xyz.device):
+        s = int(torch.cuda.current_stream().cuda_stream)
+        if kind == "full":
+            out = torch.empty((max(n, 0), 11), dtype=torch.float32, device=xyz.device)
+            _ext._dev_compute_features(xyz.data_ptr(), xyz.shape[0], nn.data_ptr(), nn.shape[0], nn_ptr.data_ptr(),
+                                       n, int(args[0]), out.data_ptr(), s)
+        elif kind == "multi":
+            scales = [int(v) for v in args[0]]
+            out = torch.empty((max(n, 0), len(scales), 11), dtype=torch.float32, device=xyz.device)
+            _ext._dev_compute_features_multiscale(xyz.data_ptr(), xyz.shape[0], nn.data_ptr(), nn.shape[0],
+                                                  nn_ptr.data_ptr(), n, scales, out.data_ptr(), s)
+        else:
+            out = torch.empty((max(n, 0), 12), dtype=torch.float32, device=xyz.device)
+            _ext._dev_compute_features_optimal(xyz.data_ptr(), xyz.shape[0], nn.data_ptr(), nn.shape[0],
+                                               nn_ptr.data_ptr(), n, int(args[0]), int(args[1]), int(args[2]),
+                                               out.data_ptr(), s)
+        _finish(check, s)
+    return out
+
+
+# --------------------------------------------------------------- public API
+def compute_features(xyz, nn, nn_ptr, k_min=1, verbose=False, *, check=True):
+    """include/pgeof.hpp:75-117 -- (n_points, 11) float32 features from CSR neighbours."""
+    if _is_torch(xyz):
+        return _dev_features("full", xyz, nn, nn_ptr, (k_min,), check)
+    return _ext.compute_features(xyz, nn, nn_ptr, k_min, verbose)
+
+
+def compute_features_multiscale(xyz, nn, nn_ptr, k_scales, verbose=False, *, check=True):
+    """include/pgeof.hpp:123-211 -- (n_points, n_scales, 11) float32 features."""
+    if _is_torch(xyz):
+        return _dev_features("multi", xyz, nn, nn_ptr, (k_scales,), check)
+    return _ext.compute_features_multiscale(xyz, nn, nn_ptr, k_scales, verbose)
+
+
+def compute_features_optimal(xyz, nn, nn_ptr, k_min=1, k_step=1, k_min_search=1, verbose=False, *, check=True):
+    """include/pgeof.hpp:243-310 -- (n_points, 12) float32, column 11 = optimal k."""
+    if _is_torch(xyz):
+        return _dev_features("optimal", xyz, nn, nn_ptr, (k_min, k_step, k_min_search), check)
+    return _ext.compute_features_optimal(xyz, nn, nn_ptr, k_min, k_step, k_min_search, verbose)
+
+
+def knn_search(data, query, knn):
+    """include/nn_search.hpp:31-67 -- (uint32 indices, float32 squared distances), (n_query, knn)."""
+    if _is_torch(data):
+        torch = _sys.modules["torch"]
+        _dev_cloud(data, "data")
+        _dev_cloud(query, "query")
+        with torch.cuda.device(data.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            idx = _uint32_empty(torch, (query.shape[0], int(knn)), data.device)
+            d2 = torch.empty((query.shape[0], int(knn)), dtype=torch.float32, device=data.device)
+            _ext._dev_knn_search(data.data_ptr(), data.shape[0], query.data_ptr(), query.shape[0], int(knn),
+                                 idx.data_ptr(), d2.data_ptr(), s)
+        return idx, d2
+    return _ext.knn_search(data, query, knn)
+
+
+def radius_search(data, query, search_radius, max_knn):
+    """include/nn_search.hpp:85-132 -- (int32 indices, -1 = none; float32 squared distances)."""
+    if _is_torch(data):
+        torch = _sys.modules["torch"]
+        _dev_cloud(data, "data")
+        _dev_cloud(query, "query")
+        with torch.cuda.device(data.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            idx = torch.empty((query.shape[0], int(max_knn)), dtype=torch.int32, device=data.device)
+            d2 = torch.empty((query.shape[0], int(max_knn)), dtype=torch.float32, device=data.device)
+            _ext._dev_radius_search(data.data_ptr(), data.shape[0], query.data_ptr(), query.shape[0],
+                                    float(search_radius), int(max_knn), idx.data_ptr(), d2.data_ptr(), s)
+        return idx, d2
+    return _ext.radius_search(data, query, search_radius, max_knn)
+
+
+def compute_features_selected(xyz, search_radius, max_knn, selected_features):
+    """include/pgeof.hpp:325-375 -- (n, len(selected_features)) in xyz's precision."""
+    if _is_torch(xyz):
+        torch = _sys.modules["torch"]
+        f64 = xyz.dtype == torch.float64
+        _dev_cloud(xyz, "xyz", "float64" if f64 else "float32")
+        ids = [int(v) for v in selected_features]
+        with torch.cuda.device(xyz.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            out = torch.empty((xyz.shape[0], len(ids)), dtype=xyz.dtype, device=xyz.device)
+            _ext._dev_compute_features_selected(xyz.data_ptr(), xyz.shape[0], float(search_radius), int(max_knn),
+                                                ids, f64, out.data_ptr(), s)
+        return out
+    return _ext.compute_features_selected(xyz, search_radius, max_knn, selected_features)

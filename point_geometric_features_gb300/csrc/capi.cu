@@ -1,0 +1,508 @@
+// capi.cu -- the extern "C" entry points of libpgeof_cuda (include/pgeof_cuda.h):
+// argument checks with the reference's error conditions, per-device state
+// (memory pool, data-error word), the asynchronous device-pointer family and
+// the synchronous host-pointer family that the Python binding uses.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace pgeof {
+
+std::atomic<uint64_t> g_launch_count{0};
+
+namespace {
+
+thread_local std::string t_last_error;
+thread_local uint32_t* t_error_word_override = nullptr;
+std::atomic<int> g_eig_order{0};
+
+struct DevState {
+    std::once_flag once;
+    int status = PGEOF_OK;
+    std::string msg;
+    DeviceInfo info;
+    cudaMemPool_t pool = nullptr;
+    uint32_t* err_word = nullptr;
+};
+constexpr int kMaxDevices = 64;
+DevState g_dev[kMaxDevices];
+
+void init_device(DevState& st, int dev) {
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) {
+        st.status = PGEOF_ERR_NO_DEVICE;
+        st.msg = std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e);
+        return;
+    }
+    if (!(prop.major == 10 && prop.minor == 3)) {
+        st.status = PGEOF_ERR_NO_DEVICE;
+        st.msg = "libpgeof_cuda is built for sm_103a (GB300); device " + std::to_string(dev) + " is " + prop.name +
+                 " (sm_" + std::to_string(prop.major) + std::to_string(prop.minor) + ")";
+        return;
+    }
+    st.info.device = dev;
+    st.info.sm_count = prop.multiProcessorCount;
+    st.info.max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    e = cudaMemPoolCreate(&st.pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        e = cudaMemPoolSetAttribute(st.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&st.err_word, 256);
+    if (e == cudaSuccess) e = cudaMemset(st.err_word, 0, 256);
+    if (e != cudaSuccess) {
+        st.status = PGEOF_ERR_CUDA;
+        st.msg = std::string("device initialisation: ") + cudaGetErrorString(e);
+    }
+}
+
+int device_state(DevState** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        (void)cudaGetLastError();
+        return fail(PGEOF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    DevState& st = g_dev[dev];
+    std::call_once(st.once, init_device, std::ref(st), dev);
+    if (st.status != PGEOF_OK) return fail(st.status, st.msg);
+    *out = &st;
+    return PGEOF_OK;
+}
+
+cudaStream_t host_stream() {
+    // one non-blocking stream per host thread and device for the host-pointer API
+    thread_local cudaStream_t streams[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!streams[dev]) cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking);
+    return streams[dev];
+}
+
+// Per-call data-error word for host-pointer calls (no cross-talk between threads).
+struct CallErrors {
+    Scratch word;
+    cudaStream_t s;
+    explicit CallErrors(cudaStream_t stream) : s(stream) {}
+    int begin() {
+        PGEOF_TRY(word.alloc(16, s));
+        PGEOF_CUDA_TRY(cudaMemsetAsync(word.p, 0, 16, s));
+        t_error_word_override = word.as<uint32_t>();
+        return PGEOF_OK;
+    }
+    ~CallErrors() { t_error_word_override = nullptr; }
+    // after the stream is synchronised
+    int check() {
+        uint32_t bits = 0;
+        PGEOF_CUDA_TRY(cudaMemcpy(&bits, word.p, sizeof(bits), cudaMemcpyDeviceToHost));
+        return bits_status(bits);
+    }
+    static int bits_status(uint32_t bits) {
+        if (bits & ERR_NN_RANGE) return fail(PGEOF_ERR_DATA, "nn holds an index >= the number of points in xyz");
+        if (bits & ERR_PTR_RANGE)
+            return fail(PGEOF_ERR_DATA, "nn_ptr must be non-decreasing and its values must not exceed len(nn)");
+        if (bits & ERR_INTERNAL) return fail(PGEOF_ERR_INTERNAL, "neighbour selection exceeded its refinement bound");
+        return PGEOF_OK;
+    }
+};
+
+template <class T>
+int upload(Scratch& dst, const T* src, uint64_t count, cudaStream_t s) {
+    PGEOF_TRY(dst.alloc(count * sizeof(T), s));
+    if (count) PGEOF_CUDA_TRY(cudaMemcpyAsync(dst.p, src, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    return PGEOF_OK;
+}
+template <class T>
+int download(T* dst, const Scratch& src, uint64_t count, cudaStream_t s) {
+    if (count) PGEOF_CUDA_TRY(cudaMemcpyAsync(dst, src.p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    return PGEOF_OK;
+}
+
+int finish_host(CallErrors& ce, cudaStream_t s) {
+    PGEOF_CUDA_TRY(cudaStreamSynchronize(s));
+    return ce.check();
+}
+
+// ------------------------------------------------------------ validation
+constexpr uint64_t kMaxPoints = 0xfffffffeull;
+
+int check_cloud(int64_t n, const char* what) {
+    if (n < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, std::string(what) + " has a negative size");
+    if ((uint64_t)n > kMaxPoints) return fail(PGEOF_ERR_INVALID_ARGUMENT, std::string(what) + " exceeds 2^32-2 points");
+    return PGEOF_OK;
+}
+
+int check_csr(int64_t n_xyz, int64_t nnz, int64_t n_points) {
+    PGEOF_TRY(check_cloud(n_xyz, "xyz"));
+    if (n_points < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn_ptr must hold at least one entry");
+    if ((uint64_t)n_points > kMaxPoints) return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn_ptr is too long");
+    if (nnz < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn has a negative size");
+    return PGEOF_OK;
+}
+
+// include/pgeof.hpp:123-132
+bool check_scales(const uint32_t* k_scales, int64_t n) {
+    uint32_t prev = 1;
+    for (int64_t i = 0; i < n; ++i) {
+        if (k_scales[i] < prev) return false;
+        prev = k_scales[i];
+    }
+    return true;
+}
+
+// ------------------------------------------------------------ device impls
+int knn_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_query, uint32_t knn,
+             uint32_t* indices, float* sqr_dist, bool query_is_data, cudaStream_t s) {
+    if (n_query == 0 || knn == 0) return PGEOF_OK;
+    GridIndex<float> grid;
+    PGEOF_TRY(build_grid<float>(data, n_data, knn, 0.0f, 0.0f, grid, s));
+    const SPoint<float>* q = grid.pts;
+    Scratch qmem;
+    if (!query_is_data) PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, const_cast<SPoint<float>**>(&q), s));
+    SearchOut<float> out;
+    out.indices = indices;
+    out.sqr_dist = sqr_dist;
+    return launch_search<float>(grid, q, n_query, MODE_KNN, knn, 0.0f, out, s);
+}
+
+int radius_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_query, float radius,
+                uint32_t max_knn, int32_t* indices, float* sqr_dist, bool query_is_data, cudaStream_t s) {
+    if (n_query == 0 || max_knn == 0) return PGEOF_OK;
+    GridIndex<float> grid;
+    const float r = std::fabs(radius);
+    PGEOF_TRY(build_grid<float>(data, n_data, max_knn, r / 4.0f, r, grid, s));
+    const SPoint<float>* q = grid.pts;
+    Scratch qmem;
+    if (!query_is_data) PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, const_cast<SPoint<float>**>(&q), s));
+    SearchOut<float> out;
+    out.indices = indices;
+    out.sqr_dist = sqr_dist;
+    out.radius_fill_last = true;
+    return launch_search<float>(grid, q, n_query, MODE_RADIUS, max_knn, radius, out, s);
+}
+
+int features_impl(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* nn_ptr,
+                  uint64_t n_points, int kind, uint64_t k_min, const uint32_t* scales, int64_t n_scales,
+                  uint32_t k_step, uint32_t k_min_search, float* out, cudaStream_t s) {
+    if (n_points == 0) return PGEOF_OK;
+    Scratch xyz4;
+    PGEOF_TRY(xyz4.alloc(std::max<uint64_t>(n_xyz, 1) * sizeof(float4), s));
+    PGEOF_TRY(pad_xyz(xyz, n_xyz, xyz4.as<float4>(), s));
+    if (kind == 2)
+        return launch_optimal(xyz4.as<float4>(), n_xyz, nn, nnz, nn_ptr, n_points, (uint32_t)k_min, k_step,
+                              k_min_search, out, nullptr, s);
+    if (kind == 1 && n_scales == 0) return PGEOF_OK;
+    return launch_features(xyz4.as<float4>(), n_xyz, nn, nnz, nn_ptr, n_points, kind == 0, k_min, scales,
+                           (int)n_scales, out, nullptr, s);
+}
+
+template <typename T>
+int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const int32_t* ids, int64_t n_ids, T* out,
+                  cudaStream_t s) {
+    if (n == 0 || n_ids == 0) return PGEOF_OK;
+    GridIndex<T> grid;
+    const float r = (float)std::fabs((double)radius);
+    const uint32_t k_search = std::max<uint32_t>(max_knn, 1u);
+    PGEOF_TRY(build_grid<T>(xyz, n, k_search, r / 4.0f, r, grid, s));
+    Scratch nbr, found;
+    PGEOF_TRY(nbr.alloc(n * (uint64_t)k_search * sizeof(int32_t), s));
+    PGEOF_TRY(found.alloc(n * sizeof(uint32_t), s));
+    SearchOut<T> so;
+    so.indices = nbr.p;
+    so.sqr_dist = nullptr;
+    so.found = found.as<uint32_t>();
+    so.radius_fill_last = false;
+    PGEOF_TRY(launch_search<T>(grid, grid.pts, n, MODE_RADIUS, k_search, radius, so, s));
+    return launch_selected_pca<T>(xyz, n, nbr.as<int32_t>(), found.as<uint32_t>(), max_knn, ids, (int)n_ids, out,
+                                  s);
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { t_last_error = msg; }
+int fail(int status, const std::string& msg) {
+    t_last_error = msg;
+    return status;
+}
+int check_launch(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(PGEOF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return PGEOF_OK;
+}
+int current_device_info(const DeviceInfo** out) {
+    DevState* st;
+    PGEOF_TRY(device_state(&st));
+    *out = &st->info;
+    return PGEOF_OK;
+}
+uint32_t* device_error_word() {
+    if (t_error_word_override) return t_error_word_override;
+    DevState* st = nullptr;
+    if (device_state(&st) != PGEOF_OK) return nullptr;
+    return st->err_word;
+}
+int scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+    DevState* st;
+    PGEOF_TRY(device_state(&st));
+    PGEOF_CUDA_TRY(cudaMallocFromPoolAsync(p, bytes, st->pool, s));
+    return PGEOF_OK;
+}
+void scratch_free(void* p, cudaStream_t s) { cudaFreeAsync(p, s); }
+int eig_order() { return g_eig_order.load(std::memory_order_relaxed); }
+
+}  // namespace pgeof
+
+using namespace pgeof;
+
+namespace {
+template <typename T>
+int host_selected(const T* xyz, int64_t n, T radius, uint32_t max_knn, const int32_t* ids, int64_t n_ids,
+                         T* features) {
+    PGEOF_TRY(check_cloud(n, "xyz"));
+    if (n_ids < 0 || (n_ids > 0 && !ids)) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid selected feature list");
+    if (n == 0 || n_ids == 0) return PGEOF_OK;
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    Scratch d_xyz, d_out;
+    PGEOF_TRY(upload(d_xyz, xyz, 3ull * n, s));
+    const uint64_t cnt = (uint64_t)n * n_ids;
+    PGEOF_TRY(d_out.alloc(cnt * sizeof(T), s));
+    PGEOF_TRY(selected_impl<T>(d_xyz.as<T>(), n, radius, max_knn, ids, n_ids, d_out.as<T>(), s));
+    PGEOF_TRY(download(features, d_out, cnt, s));
+    return finish_host(ce, s);
+}
+
+}  // namespace
+
+// =========================================================================
+extern "C" {
+
+int pgeof_abi_version(void) { return PGEOF_ABI_VERSION; }
+
+const char* pgeof_status_string(int status) {
+    switch (status) {
+        case PGEOF_OK: return "ok";
+        case PGEOF_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PGEOF_ERR_DATA: return "invalid neighbour data";
+        case PGEOF_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case PGEOF_ERR_CUDA: return "CUDA error";
+        case PGEOF_ERR_NO_DEVICE: return "no usable GB300 device";
+        case PGEOF_ERR_INTERNAL: return "internal bound exceeded";
+        default: return "unknown status";
+    }
+}
+
+const char* pgeof_last_error_message(void) { return t_last_error.c_str(); }
+
+uint64_t pgeof_kernel_launch_count(void) { return g_launch_count.load(); }
+
+int pgeof_set_eig_order(int order) {
+    if (order != 0 && order != 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "eig order must be 0 or 1");
+    g_eig_order.store(order);
+    return PGEOF_OK;
+}
+int pgeof_get_eig_order(void) { return g_eig_order.load(); }
+
+int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits) {
+    DevState* st;
+    PGEOF_TRY(device_state(&st));
+    PGEOF_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t v = 0;
+    PGEOF_CUDA_TRY(cudaMemcpy(&v, st->err_word, sizeof(v), cudaMemcpyDeviceToHost));
+    PGEOF_CUDA_TRY(cudaMemset(st->err_word, 0, sizeof(v)));
+    if (bits) *bits = v;
+    return PGEOF_OK;
+}
+
+// ---------------------------------------------------------------- device API
+int pgeof_knn_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query, uint32_t knn,
+                         uint32_t* indices, float* sqr_dist, pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n_data, "data"));
+    PGEOF_TRY(check_cloud(n_query, "query"));
+    if ((int64_t)knn > n_data)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "knn size is greater than the data point cloud size");
+    return knn_impl(data, n_data, query, n_query, knn, indices, sqr_dist, data == query && n_data == n_query,
+                    (cudaStream_t)stream);
+}
+
+int pgeof_radius_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                            float search_radius, uint32_t max_knn, int32_t* indices, float* sqr_dist,
+                            pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n_data, "data"));
+    PGEOF_TRY(check_cloud(n_query, "query"));
+    if ((int64_t)max_knn > n_data)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "max knn size is greater than the data point cloud size");
+    return radius_impl(data, n_data, query, n_query, search_radius, max_knn, indices, sqr_dist,
+                       data == query && n_data == n_query, (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                               const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features,
+                               pgeof_stream_t stream) {
+    if (k_min < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min should be > 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return features_impl(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 0, k_min, nullptr, 0, 0, 0, features,
+                         (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                          const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                          int64_t n_scales, float* features, pgeof_stream_t stream) {
+    if (n_scales < 0 || (n_scales > 0 && !k_scales) || !check_scales(k_scales, n_scales))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales should be > 1 and sorted in ascending order");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return features_impl(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 1, 1, k_scales, n_scales, 0, 0, features,
+                         (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                       const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
+                                       uint32_t k_min_search, float* features, pgeof_stream_t stream) {
+    if (k_min < 1 && k_min_search < 1)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min and k_min_search should be > 1");
+    if (k_step < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_step should be >= 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return features_impl(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 2, k_min, nullptr, 0, k_step, k_min_search,
+                         features, (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
+                                        const int32_t* selected, int64_t n_selected, float* features,
+                                        pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n, "xyz"));
+    if (n_selected < 0 || (n_selected > 0 && !selected))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid selected feature list");
+    return selected_impl<float>(xyz, n, search_radius, max_knn, selected, n_selected, features,
+                                (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_selected_f64(const double* xyz, int64_t n, double search_radius, uint32_t max_knn,
+                                        const int32_t* selected, int64_t n_selected, double* features,
+                                        pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n, "xyz"));
+    if (n_selected < 0 || (n_selected > 0 && !selected))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid selected feature list");
+    return selected_impl<double>(xyz, n, search_radius, max_knn, selected, n_selected, features,
+                                 (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------- host API
+int pgeof_host_knn_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                              uint32_t knn, uint32_t* indices, float* sqr_dist) {
+    PGEOF_TRY(check_cloud(n_data, "data"));
+    PGEOF_TRY(check_cloud(n_query, "query"));
+    if ((int64_t)knn > n_data)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "knn size is greater than the data point cloud size");
+    if (n_query == 0 || knn == 0) return PGEOF_OK;
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    const bool same = data == query && n_data == n_query;
+    Scratch d_data, d_query, d_idx, d_d2;
+    PGEOF_TRY(upload(d_data, data, 3ull * n_data, s));
+    if (!same) PGEOF_TRY(upload(d_query, query, 3ull * n_query, s));
+    const uint64_t cnt = (uint64_t)n_query * knn;
+    PGEOF_TRY(d_idx.alloc(cnt * sizeof(uint32_t), s));
+    PGEOF_TRY(d_d2.alloc(cnt * sizeof(float), s));
+    PGEOF_TRY(knn_impl(d_data.as<float>(), n_data, same ? d_data.as<float>() : d_query.as<float>(), n_query, knn,
+                       d_idx.as<uint32_t>(), d_d2.as<float>(), same, s));
+    PGEOF_TRY(download(indices, d_idx, cnt, s));
+    PGEOF_TRY(download(sqr_dist, d_d2, cnt, s));
+    return finish_host(ce, s);
+}
+
+int pgeof_host_radius_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                                 float search_radius, uint32_t max_knn, int32_t* indices, float* sqr_dist) {
+    PGEOF_TRY(check_cloud(n_data, "data"));
+    PGEOF_TRY(check_cloud(n_query, "query"));
+    if ((int64_t)max_knn > n_data)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "max knn size is greater than the data point cloud size");
+    if (n_query == 0 || max_knn == 0) return PGEOF_OK;
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    const bool same = data == query && n_data == n_query;
+    Scratch d_data, d_query, d_idx, d_d2;
+    PGEOF_TRY(upload(d_data, data, 3ull * n_data, s));
+    if (!same) PGEOF_TRY(upload(d_query, query, 3ull * n_query, s));
+    const uint64_t cnt = (uint64_t)n_query * max_knn;
+    PGEOF_TRY(d_idx.alloc(cnt * sizeof(int32_t), s));
+    PGEOF_TRY(d_d2.alloc(cnt * sizeof(float), s));
+    PGEOF_TRY(radius_impl(d_data.as<float>(), n_data, same ? d_data.as<float>() : d_query.as<float>(), n_query,
+                          search_radius, max_knn, d_idx.as<int32_t>(), d_d2.as<float>(), same, s));
+    PGEOF_TRY(download(indices, d_idx, cnt, s));
+    PGEOF_TRY(download(sqr_dist, d_d2, cnt, s));
+    return finish_host(ce, s);
+}
+
+static int host_features(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz, const uint32_t* nn_ptr,
+                         int64_t n_points, int kind, uint64_t k_min, const uint32_t* scales, int64_t n_scales,
+                         uint32_t k_step, uint32_t k_min_search, float* features, uint64_t row_width) {
+    if (n_points == 0 || row_width == 0) return PGEOF_OK;
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    Scratch d_xyz, d_nn, d_ptr, d_out;
+    PGEOF_TRY(upload(d_xyz, xyz, 3ull * n_xyz, s));
+    PGEOF_TRY(upload(d_nn, nn, (uint64_t)nnz, s));
+    PGEOF_TRY(upload(d_ptr, nn_ptr, (uint64_t)n_points + 1, s));
+    const uint64_t cnt = (uint64_t)n_points * row_width;
+    PGEOF_TRY(d_out.alloc(cnt * sizeof(float), s));
+    PGEOF_TRY(features_impl(d_xyz.as<float>(), n_xyz, d_nn.as<uint32_t>(), nnz, d_ptr.as<uint32_t>(), n_points, kind,
+                            k_min, scales, n_scales, k_step, k_min_search, d_out.as<float>(), s));
+    PGEOF_TRY(download(features, d_out, cnt, s));
+    return finish_host(ce, s);
+}
+
+int pgeof_host_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                    const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features) {
+    if (k_min < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min should be > 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 0, k_min, nullptr, 0, 0, 0, features, 11);
+}
+
+int pgeof_host_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                               const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                               int64_t n_scales, float* features) {
+    if (n_scales < 0 || (n_scales > 0 && !k_scales) || !check_scales(k_scales, n_scales))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales should be > 1 and sorted in ascending order");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 1, 1, k_scales, n_scales, 0, 0, features,
+                         11ull * (uint64_t)n_scales);
+}
+
+int pgeof_host_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                            const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min,
+                                            uint32_t k_step, uint32_t k_min_search, float* features) {
+    if (k_min < 1 && k_min_search < 1)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min and k_min_search should be > 1");
+    if (k_step < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_step should be >= 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 2, k_min, nullptr, 0, k_step, k_min_search,
+                         features, 12);
+}
+
+int pgeof_host_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
+                                             const int32_t* selected, int64_t n_selected, float* features) {
+    return host_selected<float>(xyz, n, search_radius, max_knn, selected, n_selected, features);
+}
+
+int pgeof_host_compute_features_selected_f64(const double* xyz, int64_t n, double search_radius,
+                                             uint32_t max_knn, const int32_t* selected, int64_t n_selected,
+                                             double* features) {
+    return host_selected<double>(xyz, n, search_radius, max_knn, selected, n_selected, features);
+}
+
+}  // extern "C"

@@ -1,0 +1,310 @@
+// eig3.cuh -- per-neighbourhood PCA on the device: symmetric 3x3 eigen
+// decomposition and the feature epilogues of pgeof (include/pca.hpp).
+//
+// Eigen-solver design. The covariance is formed in float exactly as the
+// reference does (include/pca.hpp:75-76, see the feature kernels). It is then
+// diagonalised by cyclic Jacobi rotations (Golub & Van Loan, "Matrix
+// Computations", sec. 8.5) in float. Jacobi is backward stable, so the float
+// eigenvectors are accurate to ~eps*|A|/gap; when the smallest eigen-gap is
+// below kGapResolve*|A| the same float covariance is diagonalised again in
+// double with exactly the arithmetic of the CPU oracle's solver (explicit
+// round-to-nearest ops, no FMA), so ill-conditioned neighbourhoods reproduce
+// the exact solution of the float covariance instead of float noise. Eigenpairs
+// are then ordered as Eigen's SelfAdjointEigenSolver returns them (ascending;
+// for equal values the first minimum stays first), because the reference feeds
+// them to the formulas unsorted (pca.hpp:79-97).
+#pragma once
+
+#include "common.cuh"
+
+namespace pgeof {
+
+// Smallest relative eigen-gap handled by the float solver alone.
+constexpr float kGapResolve = 3e-3f;
+
+template <typename T>
+struct Pca {
+    T val[3];   // eigenvalues, clamped >= 0, in the order the formulas use
+    T v[3][3];  // v[r][c]: row r of eigenvector c (c = 0, 1, 2 -> v0, v1, v2)
+};
+
+template <typename T>
+struct Cov {
+    T xx, xy, xz, yy, yz, zz;
+};
+
+// One Jacobi rotation annihilating a[P][Q] (P < Q). Mirrors the CPU oracle's
+// solver operation for operation (explicit rounding, no fused multiply-add).
+template <int P, int Q, typename T, bool VEC>
+__device__ __forceinline__ void jacobi_rotate(T (&a)[3][3], T (&v)[3][3], bool late) {
+    using O = XOps<T>;
+    constexpr int R = 3 - P - Q;
+    const T apq = a[P][Q];
+    if (apq == T(0)) return;
+    const T g = O::mul(T(100), fabs(apq));
+    if (late && O::add(fabs(a[P][P]), g) == fabs(a[P][P]) && O::add(fabs(a[Q][Q]), g) == fabs(a[Q][Q])) {
+        a[P][Q] = a[Q][P] = T(0);
+        return;
+    }
+    const T h = O::sub(a[Q][Q], a[P][P]);
+    T t;
+    if (O::add(fabs(h), g) == fabs(h)) {
+        t = O::div(apq, h);
+    } else {
+        const T theta = O::div(O::mul(T(0.5), h), apq);
+        t = O::div(T(1), O::add(fabs(theta), O::sqrt_(O::add(T(1), O::mul(theta, theta)))));
+        if (theta < T(0)) t = -t;
+    }
+    const T c = O::div(T(1), O::sqrt_(O::add(T(1), O::mul(t, t))));
+    const T s = O::mul(t, c);
+    const T tau = O::div(s, O::add(T(1), c));
+    a[P][P] = O::sub(a[P][P], O::mul(t, apq));
+    a[Q][Q] = O::add(a[Q][Q], O::mul(t, apq));
+    a[P][Q] = a[Q][P] = T(0);
+    const T arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = O::sub(arp, O::mul(s, O::add(arq, O::mul(tau, arp))));
+    a[R][Q] = a[Q][R] = O::add(arq, O::mul(s, O::sub(arp, O::mul(tau, arq))));
+    if (VEC) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const T vkp = v[k][P], vkq = v[k][Q];
+            v[k][P] = O::sub(vkp, O::mul(s, O::add(vkq, O::mul(tau, vkp))));
+            v[k][Q] = O::add(vkq, O::mul(s, O::sub(vkp, O::mul(tau, vkq))));
+        }
+    }
+}
+
+// Cyclic Jacobi. EXACT=true runs to convergence like the oracle (64 sweeps at
+// most); EXACT=false stops once the off-diagonal mass is below float
+// resolution. Returns the number of sweeps that rotated something.
+template <typename T, bool VEC, bool EXACT>
+__device__ __forceinline__ int jacobi3(T (&a)[3][3], T (&v)[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? T(1) : T(0);
+    int sweeps = 0;
+    const int max_sweeps = EXACT ? 64 : 16;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (a[0][1] == T(0) && a[0][2] == T(0) && a[1][2] == T(0)) break;
+        if (!EXACT) {
+            const T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+            const T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+            if (sweep >= 2 && off <= T(1e-9) * scale) break;
+        }
+        ++sweeps;
+        const bool late = sweep > 4;
+        jacobi_rotate<0, 1, T, VEC>(a, v, late);
+        jacobi_rotate<0, 2, T, VEC>(a, v, late);
+        jacobi_rotate<1, 2, T, VEC>(a, v, late);
+    }
+    return sweeps;
+}
+
+template <int I, int K, typename T>
+__device__ __forceinline__ void swap_cols(T (&w)[3], T (&v)[3][3]) {
+    const T t = w[I];
+    w[I] = w[K];
+    w[K] = t;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const T u = v[r][I];
+        v[r][I] = v[r][K];
+        v[r][K] = u;
+    }
+}
+
+// Eigen's ascending order: position i takes the FIRST minimum of w[i..2].
+template <typename T>
+__device__ __forceinline__ void sort_ascending(T (&w)[3], T (&v)[3][3]) {
+    int k = 0;
+    if (w[1] < w[k]) k = 1;
+    if (w[2] < w[k]) k = 2;
+    if (k == 1) swap_cols<0, 1>(w, v);
+    if (k == 2) swap_cols<0, 2>(w, v);
+    if (w[2] < w[1]) swap_cols<1, 2>(w, v);
+}
+
+template <typename T>
+__device__ __forceinline__ void load_cov(const Cov<T>& c, T (&a)[3][3]) {
+    a[0][0] = c.xx;
+    a[0][1] = a[1][0] = c.xy;
+    a[0][2] = a[2][0] = c.xz;
+    a[1][1] = c.yy;
+    a[1][2] = a[2][1] = c.yz;
+    a[2][2] = c.zz;
+}
+
+// Finish: order (ascending or reversed), clamp >= 0 (std::max(ev, 0)), flip v2
+// into z >= 0 (pca.hpp:85-96).
+template <typename T, typename S>
+__device__ __forceinline__ void finish_pca(const S (&w)[3], const S (&v)[3][3], int order, Pca<T>& out) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int src = order ? 2 - i : i;
+        const T ev = (T)w[src];
+        out.val[i] = (ev < T(0)) ? T(0) : ev;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) out.v[r][i] = (T)v[r][src];
+    }
+    if (out.v[2][2] < T(0)) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) out.v[r][2] = out.v[r][2] * T(-1);
+    }
+}
+
+// Double-precision solve of a covariance, identical to the oracle's solver.
+template <typename T>
+__device__ __noinline__ void pca_solve_f64(const Cov<T> cov, int order, Pca<T>* out) {
+    double a[3][3], v[3][3], w[3];
+    a[0][0] = (double)cov.xx;
+    a[0][1] = a[1][0] = (double)cov.xy;
+    a[0][2] = a[2][0] = (double)cov.xz;
+    a[1][1] = (double)cov.yy;
+    a[1][2] = a[2][1] = (double)cov.yz;
+    a[2][2] = (double)cov.zz;
+    jacobi3<double, true, true>(a, v);
+    w[0] = a[0][0];
+    w[1] = a[1][1];
+    w[2] = a[2][2];
+    sort_ascending(w, v);
+    finish_pca<T, double>(w, v, order, *out);
+}
+
+// Float covariance -> PCA. Counts the neighbourhoods re-solved in double.
+__device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, Pca<float>& out, bool& resolved) {
+    float a[3][3], v[3][3], w[3];
+    load_cov(cov, a);
+    const int sweeps = jacobi3<float, true, false>(a, v);
+    w[0] = a[0][0];
+    w[1] = a[1][1];
+    w[2] = a[2][2];
+    sort_ascending(w, v);
+    const float gap = fminf(w[1] - w[0], w[2] - w[1]);
+    const float scale = fmaxf(fabsf(w[0]), fabsf(w[2]));
+    resolved = false;
+    if (sweeps > 0 && gap < kGapResolve * scale) {
+        // ill-conditioned eigenvectors: exact solve of the same float matrix
+        resolved = true;
+        pca_solve_f64<float>(cov, order, &out);
+        return;
+    }
+    finish_pca<float, float>(w, v, order, out);
+}
+
+// Eigenvalues only, float (for eigentropy scans). Approximate rotations are fine
+// here: the scan only ranks candidates, the winner is re-evaluated exactly.
+__device__ __forceinline__ void eigvals_f32(const Cov<float>& cov, float (&w)[3]) {
+    float a[3][3], v[3][3];
+    load_cov(cov, a);
+    jacobi3<float, false, false>(a, v);
+    w[0] = a[0][0];
+    w[1] = a[1][1];
+    w[2] = a[2][2];
+    // ascending (values only)
+    float t;
+    if (w[1] < w[0]) { t = w[0]; w[0] = w[1]; w[1] = t; }
+    if (w[2] < w[1]) { t = w[1]; w[1] = w[2]; w[2] = t; }
+    if (w[1] < w[0]) { t = w[0]; w[0] = w[1]; w[1] = t; }
+}
+
+// --------------------------------------------------------------- epilogues
+template <typename T>
+__device__ __forceinline__ T dev_pow(T x, T y);
+template <>
+__device__ __forceinline__ float dev_pow<float>(float x, float y) { return powf(x, y); }
+template <>
+__device__ __forceinline__ double dev_pow<double>(double x, double y) { return pow(x, y); }
+template <typename T>
+__device__ __forceinline__ T dev_log(T x);
+template <>
+__device__ __forceinline__ float dev_log<float>(float x) { return logf(x); }
+template <>
+__device__ __forceinline__ double dev_log<double>(double x) { return log(x); }
+
+// include/pca.hpp:140-150
+template <typename T>
+__device__ __forceinline__ T eigentropy_of(const T (&val)[3]) {
+    using O = XOps<T>;
+    const T eps = T(1e-3);
+    const T val_sum = O::add(O::add(O::add(val[0], val[1]), val[2]), eps);
+    const T e0 = O::div(val[0], val_sum);
+    const T e1 = O::div(val[1], val_sum);
+    const T e2 = O::div(val[2], val_sum);
+    T r = O::mul(-e0, dev_log<T>(O::add(e0, eps)));
+    r = O::sub(r, O::mul(e1, dev_log<T>(O::add(e1, eps))));
+    r = O::sub(r, O::mul(e2, dev_log<T>(O::add(e2, eps))));
+    return r;
+}
+
+// include/pca.hpp:189-199
+template <typename T>
+__device__ __forceinline__ T verticality_pgeof(const Pca<T>& p) {
+    using O = XOps<T>;
+    T u[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+        u[j] = O::add(O::add(O::mul(p.val[0], fabs(p.v[j][0])), O::mul(p.val[1], fabs(p.v[j][1]))),
+                      O::mul(p.val[2], fabs(p.v[j][2])));
+    const T nrm = O::sqrt_(O::add(O::add(O::mul(u[0], u[0]), O::mul(u[1], u[1])), O::mul(u[2], u[2])));
+    return O::div(u[2], nrm);
+}
+
+// include/pca.hpp:160-200; writes f[0..10] in EFeatureID order.
+template <typename T>
+__device__ __forceinline__ void features11(const Pca<T>& p, T* f) {
+    using O = XOps<T>;
+    const T eps = T(1e-3);
+    const T val0 = O::sqrt_(p.val[0]);
+    const T val1 = O::sqrt_(p.val[1]);
+    const T val2 = O::sqrt_(p.val[2]);
+    const T val0_fact = O::div(T(1), O::add(val0, eps));
+    f[4] = p.v[0][2];
+    f[5] = p.v[1][2];
+    f[6] = p.v[2][2];
+    f[0] = O::mul(O::sub(val0, val1), val0_fact);
+    f[1] = O::mul(O::sub(val1, val2), val0_fact);
+    f[2] = O::mul(val2, val0_fact);
+    f[7] = val0;
+    f[8] = O::sqrt_(O::add(O::mul(val0, val1), T(1e-6)));
+    f[9] = dev_pow<T>(O::add(O::mul(O::mul(val0, val1), val2), T(1e-9)), T(1) / T(3));
+    f[10] = O::div(val2, O::add(O::add(O::add(val0, val1), val2), eps));
+    f[3] = (val0 > T(0)) ? verticality_pgeof(p) : T(0);
+}
+
+// include/pca.hpp:212-295 for one feature id (returns false = write nothing).
+template <typename T>
+__device__ __forceinline__ bool selected_feature(const Pca<T>& p, int id, T& out) {
+    using O = XOps<T>;
+    const T eps = T(1e-3);
+    const T val0 = O::sqrt_(p.val[0]);
+    const T val1 = O::sqrt_(p.val[1]);
+    const T val2 = O::sqrt_(p.val[2]);
+    const T val0_fact = O::div(T(1), O::add(val0, eps));
+    switch (id) {
+        case PGEOF_NORMAL_X: out = p.v[0][2]; return true;
+        case PGEOF_NORMAL_Y: out = p.v[1][2]; return true;
+        case PGEOF_NORMAL_Z: out = p.v[2][2]; return true;
+        case PGEOF_LINEARITY: out = O::mul(O::sub(val0, val1), val0_fact); return true;
+        case PGEOF_PLANARITY: out = O::mul(O::sub(val1, val2), val0_fact); return true;
+        case PGEOF_SCATTERING: out = O::mul(val2, val0_fact); return true;
+        case PGEOF_LENGTH: out = val0; return true;
+        // pca.hpp:252 adds the float literal 1e-6f in both precisions
+        case PGEOF_SURFACE: out = O::sqrt_(O::add(O::mul(val0, val1), (T)1e-6f)); return true;
+        case PGEOF_VOLUME:
+            out = dev_pow<T>(O::add(O::mul(O::mul(val0, val1), val2), T(1e-9)), T(1) / T(3));
+            return true;
+        case PGEOF_CURVATURE: out = O::div(val2, O::add(O::add(O::add(val0, val1), val2), eps)); return true;
+        case PGEOF_VERTICALITY_PGEOF:
+            if (val0 > T(0)) {
+                out = verticality_pgeof(p);
+                return true;
+            }
+            return false;
+        case PGEOF_VERTICALITY: out = O::sub(T(1), fabs(p.v[2][2])); return true;
+        case PGEOF_EIGENTROPY: out = eigentropy_of<T>(p.val); return true;
+        default: return false;
+    }
+}
+
+}  // namespace pgeof

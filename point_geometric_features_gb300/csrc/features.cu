@@ -1,0 +1,510 @@
+// features.cu -- fused CSR gather -> covariance -> eigen -> feature kernels for
+// compute_features, compute_features_multiscale and compute_features_optimal
+// (include/pgeof.hpp:75-117, 123-211, 243-310).
+//
+// One thread owns one point. Its neighbours are swept twice in CSR order: the
+// first sweep forms the float mean, the second the centred float products, the
+// exact operation order of include/pca.hpp:75-76 (Eigen's column sums run
+// sequentially), so the covariance is the one the reference forms. Multiscale
+// keeps one accumulator set per scale and fills every scale prefix in the same
+// two sweeps (the reference re-gathers each prefix). Output rows are staged in
+// shared memory and leave the block as one coalesced slab.
+#include "eig3.cuh"
+#include "kernels.cuh"
+
+namespace pgeof {
+
+namespace {
+
+constexpr int kFeatThreads = 128;
+constexpr int kMaxScalesPerLaunch = 8;
+
+struct FeatArgs {
+    const float4* xyz4;
+    uint32_t n_xyz;
+    const uint32_t* nn;
+    uint64_t nnz;
+    const uint32_t* ptr;
+    uint32_t n_points;
+    uint32_t k_min;      // FULL mode gate
+    int full;            // 1: compute_features (one scale = all neighbours)
+    int n_scales;        // scales handled by this launch
+    int scale_offset;    // first output scale column of this launch
+    int out_scales;      // scales per output row
+    uint32_t scales[kMaxScalesPerLaunch];
+    int order;
+    float* out;
+    uint32_t* err;
+    unsigned long long* resolved;  // neighbourhoods re-solved in double (stats)
+};
+
+__device__ __forceinline__ float4 load_nb(const FeatArgs& a, uint64_t pos, uint32_t& flags) {
+    uint32_t id = __ldg(a.nn + pos);
+    if (id >= a.n_xyz) {
+        flags |= ERR_NN_RANGE;
+        id = 0;
+    }
+    return __ldg(a.xyz4 + id);
+}
+
+template <int S>
+__global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
+    extern __shared__ float stage[];  // kFeatThreads * n_scales * 11
+    const int tid = threadIdx.x;
+    const uint32_t i = blockIdx.x * kFeatThreads + tid;
+    const int row_w = a.n_scales * 11;
+    for (int f = 0; f < row_w; ++f) stage[f * kFeatThreads + tid] = 0.0f;  // column-major staging
+
+    uint32_t flags = 0;
+    unsigned n_resolved = 0;
+    if (i < a.n_points) {
+        const uint32_t b = __ldg(a.ptr + i), e = __ldg(a.ptr + i + 1);
+        uint32_t k_nn = 0;
+        if (e < b || (uint64_t)e > a.nnz) {
+            flags |= ERR_PTR_RANGE;
+        } else {
+            k_nn = e - b;
+        }
+        uint32_t ks[S];
+        int n_active = 0;
+        uint32_t kmax = 0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            ks[s] = a.full ? k_nn : a.scales[s];
+            bool act;
+            if (a.full) {
+                act = s == 0 && k_nn >= a.k_min;
+            } else {
+                act = s < a.n_scales && k_nn >= ks[s] && n_active == s;  // break at the first short scale
+            }
+            if (act) {
+                n_active = s + 1;
+                kmax = ks[s] > kmax ? ks[s] : kmax;
+            }
+        }
+        if (n_active > 0) {
+            // sweep 1: sequential float sums -> means
+            float sx[S], sy[S], sz[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) sx[s] = sy[s] = sz[s] = 0.0f;
+            for (uint32_t j = 0; j < kmax; ++j) {
+                const float4 p = load_nb(a, (uint64_t)b + j, flags);
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    if (s < n_active && j < ks[s]) {
+                        sx[s] = FADD(sx[s], p.x);
+                        sy[s] = FADD(sy[s], p.y);
+                        sz[s] = FADD(sz[s], p.z);
+                    }
+                }
+            }
+            float mx[S], my[S], mz[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const float kk = (float)ks[s];
+                mx[s] = FDIV(sx[s], kk);
+                my[s] = FDIV(sy[s], kk);
+                mz[s] = FDIV(sz[s], kk);
+            }
+            // sweep 2: centred products, sequential sums
+            float cxx[S], cxy[S], cxz[S], cyy[S], cyz[S], czz[S];
+#pragma unroll
+            for (int s = 0; s < S; ++s) cxx[s] = cxy[s] = cxz[s] = cyy[s] = cyz[s] = czz[s] = 0.0f;
+            for (uint32_t j = 0; j < kmax; ++j) {
+                const float4 p = load_nb(a, (uint64_t)b + j, flags);
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    if (s < n_active && j < ks[s]) {
+                        const float dx = FSUB(p.x, mx[s]);
+                        const float dy = FSUB(p.y, my[s]);
+                        const float dz = FSUB(p.z, mz[s]);
+                        cxx[s] = FADD(cxx[s], FMUL(dx, dx));
+                        cxy[s] = FADD(cxy[s], FMUL(dx, dy));
+                        cxz[s] = FADD(cxz[s], FMUL(dx, dz));
+                        cyy[s] = FADD(cyy[s], FMUL(dy, dy));
+                        cyz[s] = FADD(cyz[s], FMUL(dy, dz));
+                        czz[s] = FADD(czz[s], FMUL(dz, dz));
+                    }
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                if (s < n_active) {
+                    const float kk = (float)ks[s];
+                    Cov<float> c;
+                    c.xx = FDIV(cxx[s], kk);
+                    c.xy = FDIV(cxy[s], kk);
+                    c.xz = FDIV(cxz[s], kk);
+                    c.yy = FDIV(cyy[s], kk);
+                    c.yz = FDIV(cyz[s], kk);
+                    c.zz = FDIV(czz[s], kk);
+                    Pca<float> p;
+                    bool res;
+                    pca_solve_f32(c, a.order, p, res);
+                    n_resolved += res;
+                    float f[11];
+                    features11(p, f);
+#pragma unroll
+                    for (int q = 0; q < 11; ++q) stage[(s * 11 + q) * kFeatThreads + tid] = f[q];
+                }
+            }
+        }
+    }
+    if (flags) atomicOr(a.err, flags);
+    if (a.resolved && n_resolved) atomicAdd(a.resolved, (unsigned long long)n_resolved);
+    __syncthreads();
+    // coalesced write-out of the block's rows
+    const uint32_t row0 = blockIdx.x * kFeatThreads;
+    const uint32_t rows = min((uint32_t)kFeatThreads, a.n_points - row0);
+    if (a.n_scales == a.out_scales) {
+        float* dst = a.out + (uint64_t)row0 * row_w;
+        const int total = rows * row_w;
+        for (int t = tid; t < total; t += kFeatThreads) {
+            const int r = t / row_w, c = t - r * row_w;
+            dst[t] = stage[c * kFeatThreads + r];
+        }
+    } else {
+        const int out_w = a.out_scales * 11;
+        for (int t = tid; t < (int)rows * row_w; t += kFeatThreads) {
+            const int r = t / row_w, c = t - r * row_w;
+            a.out[(uint64_t)(row0 + r) * out_w + a.scale_offset * 11 + c] = stage[c * kFeatThreads + r];
+        }
+    }
+}
+
+__global__ void pad_xyz_kernel(const float* __restrict__ xyz, uint64_t n, float4* __restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        out[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], 0.0f);
+    }
+}
+
+// ------------------------------------------------------------------ optimal
+constexpr int kOptThreads = 128;
+constexpr int kOptSlots = 64;  // eigentropy values kept per point for the near-tie pass
+
+struct OptArgs {
+    const float4* xyz4;
+    uint32_t n_xyz;
+    const uint32_t* nn;
+    uint64_t nnz;
+    const uint32_t* ptr;
+    uint32_t n_points;
+    uint32_t k_min, k_step, k_min_search;
+    int order;
+    float* out;  // (n, 12)
+    uint32_t* err;
+    unsigned long long* stats;  // [0] exact tie re-evaluations, [1] double re-solves
+};
+
+// Kahan-compensated running sum.
+struct KSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = FSUB(x, c);
+        const float t = FADD(s, y);
+        c = FSUB(FSUB(t, s), y);
+        s = t;
+    }
+};
+
+// Eigenvalues of a symmetric 3x3 by the trigonometric closed form (O. K.
+// Smith, "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961). Used only to
+// rank candidate neighbourhood sizes.
+__device__ __forceinline__ void eigvals_closed_form(const Cov<float>& c, float (&w)[3]) {
+    const float q = (c.xx + c.yy + c.zz) * (1.0f / 3.0f);
+    const float b00 = c.xx - q, b11 = c.yy - q, b22 = c.zz - q;
+    const float off = c.xy * c.xy + c.xz * c.xz + c.yz * c.yz;
+    const float p2 = (b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * off) * (1.0f / 6.0f);
+    if (!(p2 > 0.0f)) {
+        w[0] = w[1] = w[2] = q;
+        return;
+    }
+    const float p = sqrtf(p2);
+    const float det = b00 * (b11 * b22 - c.yz * c.yz) - c.xy * (c.xy * b22 - c.yz * c.xz) +
+                      c.xz * (c.xy * c.yz - b11 * c.xz);
+    float r = det / (2.0f * p2 * p);
+    r = fminf(1.0f, fmaxf(-1.0f, r));
+    const float phi = acosf(r) * (1.0f / 3.0f);
+    const float e2 = q + 2.0f * p * cosf(phi);
+    const float e0 = q + 2.0f * p * cosf(phi + 2.0943951023931953f);
+    w[0] = e0;
+    w[2] = e2;
+    w[1] = 3.0f * q - e0 - e2;
+}
+
+// Covariance of the first k neighbours exactly as include/pca.hpp:75-76.
+__device__ __forceinline__ Cov<float> literal_cov(const OptArgs& a, uint32_t b, uint32_t k, uint32_t& flags) {
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        uint32_t id = __ldg(a.nn + b + j);
+        if (id >= a.n_xyz) {
+            flags |= ERR_NN_RANGE;
+            id = 0;
+        }
+        const float4 p = __ldg(a.xyz4 + id);
+        sx = FADD(sx, p.x);
+        sy = FADD(sy, p.y);
+        sz = FADD(sz, p.z);
+    }
+    const float kk = (float)k;
+    const float mx = FDIV(sx, kk), my = FDIV(sy, kk), mz = FDIV(sz, kk);
+    float xx = 0.0f, xy = 0.0f, xz = 0.0f, yy = 0.0f, yz = 0.0f, zz = 0.0f;
+    for (uint32_t j = 0; j < k; ++j) {
+        uint32_t id = __ldg(a.nn + b + j);
+        if (id >= a.n_xyz) id = 0;
+        const float4 p = __ldg(a.xyz4 + id);
+        const float dx = FSUB(p.x, mx), dy = FSUB(p.y, my), dz = FSUB(p.z, mz);
+        xx = FADD(xx, FMUL(dx, dx));
+        xy = FADD(xy, FMUL(dx, dy));
+        xz = FADD(xz, FMUL(dx, dz));
+        yy = FADD(yy, FMUL(dy, dy));
+        yz = FADD(yz, FMUL(dy, dz));
+        zz = FADD(zz, FMUL(dz, dz));
+    }
+    Cov<float> c;
+    c.xx = FDIV(xx, kk);
+    c.xy = FDIV(xy, kk);
+    c.xz = FDIV(xz, kk);
+    c.yy = FDIV(yy, kk);
+    c.yz = FDIV(yz, kk);
+    c.zz = FDIV(zz, kk);
+    return c;
+}
+
+__device__ __forceinline__ bool evaluated(uint32_t k, uint32_t k0, uint32_t k_nn, uint32_t step) {
+    return k == k0 || k % step == 0 || k == k_nn;
+}
+
+// include/pgeof.hpp:264-299. Candidate sizes are ranked by eigentropy from
+// compensated prefix moments (O(k) gathers instead of the reference's O(k^2));
+// every size whose fast eigentropy lies within kTieBand of the fast minimum is
+// then re-evaluated from the reference's own covariance and an exact eigen
+// solve, and the smallest exact eigentropy wins (first k on equality -- the
+// reference's strict '<' scan). Features come from the winning size's
+// reference covariance.
+__global__ void __launch_bounds__(kOptThreads) optimal_kernel(const __grid_constant__ OptArgs a) {
+    constexpr float kTieBand = 3e-5f;
+    __shared__ float ent[kOptSlots * kOptThreads];
+    __shared__ float stage[12 * kOptThreads];
+    const int tid = threadIdx.x;
+    const uint32_t i = blockIdx.x * kOptThreads + tid;
+#pragma unroll
+    for (int f = 0; f < 12; ++f) stage[f * kOptThreads + tid] = 0.0f;
+    uint32_t flags = 0;
+    unsigned n_exact = 0, n_resolved = 0;
+    if (i < a.n_points) {
+        const uint32_t b = __ldg(a.ptr + i), e = __ldg(a.ptr + i + 1);
+        uint32_t k_nn = 0;
+        bool ok = true;
+        if (e < b || (uint64_t)e > a.nnz) {
+            flags |= ERR_PTR_RANGE;
+            ok = false;
+        } else {
+            k_nn = e - b;
+        }
+        if (ok && k_nn >= a.k_min && k_nn >= a.k_min_search && k_nn > 0) {
+            uint32_t k0 = max(a.k_min, a.k_min_search);
+            k0 = min(k0, k_nn);
+            // fast scan over prefix moments, shifted by the first neighbour
+            uint32_t id0 = __ldg(a.nn + b);
+            if (id0 >= a.n_xyz) {
+                flags |= ERR_NN_RANGE;
+                id0 = 0;
+            }
+            const float4 p0 = __ldg(a.xyz4 + id0);
+            KSum s1x, s1y, s1z, sxx, sxy, sxz, syy, syz, szz;
+            float best = 0.0f;
+            int slot = 0;
+            bool stored_all = true;
+            for (uint32_t k = 1; k <= k_nn; ++k) {
+                uint32_t id = __ldg(a.nn + b + k - 1);
+                if (id >= a.n_xyz) {
+                    flags |= ERR_NN_RANGE;
+                    id = 0;
+                }
+                const float4 p = __ldg(a.xyz4 + id);
+                const float dx = p.x - p0.x, dy = p.y - p0.y, dz = p.z - p0.z;
+                s1x.add(dx);
+                s1y.add(dy);
+                s1z.add(dz);
+                sxx.add(dx * dx);
+                sxy.add(dx * dy);
+                sxz.add(dx * dz);
+                syy.add(dy * dy);
+                syz.add(dy * dz);
+                szz.add(dz * dz);
+                if (k < k0 || !evaluated(k, k0, k_nn, a.k_step)) continue;
+                const float inv = 1.0f / (float)k;
+                const float mx = s1x.s * inv, my = s1y.s * inv, mz = s1z.s * inv;
+                Cov<float> c;
+                c.xx = sxx.s * inv - mx * mx;
+                c.xy = sxy.s * inv - mx * my;
+                c.xz = sxz.s * inv - mx * mz;
+                c.yy = syy.s * inv - my * my;
+                c.yz = syz.s * inv - my * mz;
+                c.zz = szz.s * inv - mz * mz;
+                float w[3];
+                eigvals_closed_form(c, w);
+                float val[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) val[q] = fmaxf(w[a.order ? 2 - q : q], 0.0f);
+                const float ent_k = eigentropy_of<float>(val);
+                if (k == k0 || ent_k < best) best = ent_k;
+                if (slot < kOptSlots) {
+                    ent[slot * kOptThreads + tid] = ent_k;
+                } else {
+                    stored_all = false;
+                }
+                ++slot;
+            }
+            // candidates within the tie band of the fast minimum
+            int n_cand = 0;
+            for (int sidx = 0; sidx < min(slot, kOptSlots); ++sidx)
+                if (ent[sidx * kOptThreads + tid] <= best + kTieBand) ++n_cand;
+            uint32_t k_opt = k0;
+            if (stored_all && n_cand == 1) {
+                // unique winner: find its k
+                int sidx = 0;
+                for (uint32_t k = k0; k <= k_nn; ++k) {
+                    if (!evaluated(k, k0, k_nn, a.k_step)) continue;
+                    if (ent[sidx * kOptThreads + tid] <= best + kTieBand) {
+                        k_opt = k;
+                        break;
+                    }
+                    ++sidx;
+                }
+            } else {
+                // near-ties (or too many sizes to store): exact re-evaluation
+                float best_exact = 0.0f;
+                bool have = false;
+                int sidx = 0;
+                for (uint32_t k = k0; k <= k_nn; ++k) {
+                    if (!evaluated(k, k0, k_nn, a.k_step)) continue;
+                    bool cand = true;
+                    if (stored_all) cand = ent[sidx * kOptThreads + tid] <= best + kTieBand;
+                    ++sidx;
+                    if (!cand) continue;
+                    ++n_exact;
+                    const Cov<float> c = literal_cov(a, b, k, flags);
+                    Pca<float> pk;
+                    pca_solve_f64<float>(c, a.order, &pk);
+                    const float ek = eigentropy_of<float>(pk.val);
+                    if (!have || ek < best_exact) {
+                        best_exact = ek;
+                        k_opt = k;
+                        have = true;
+                    }
+                }
+            }
+            const Cov<float> c = literal_cov(a, b, k_opt, flags);
+            Pca<float> p;
+            bool res;
+            pca_solve_f32(c, a.order, p, res);
+            n_resolved += res;
+            float f[11];
+            features11(p, f);
+#pragma unroll
+            for (int q = 0; q < 11; ++q) stage[q * kOptThreads + tid] = f[q];
+            stage[11 * kOptThreads + tid] = (float)k_opt;
+        }
+    }
+    if (flags) atomicOr(a.err, flags);
+    if (a.stats) {
+        if (n_exact) atomicAdd(a.stats, (unsigned long long)n_exact);
+        if (n_resolved) atomicAdd(a.stats + 1, (unsigned long long)n_resolved);
+    }
+    __syncthreads();
+    const uint32_t row0 = blockIdx.x * kOptThreads;
+    const uint32_t rows = min((uint32_t)kOptThreads, a.n_points - row0);
+    float* dst = a.out + (uint64_t)row0 * 12;
+    for (int t = tid; t < (int)rows * 12; t += kOptThreads) {
+        const int r = t / 12, c = t - r * 12;
+        dst[t] = stage[c * kOptThreads + r];
+    }
+}
+
+}  // namespace
+
+int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s) {
+    if (n == 0) return PGEOF_OK;
+    const DeviceInfo* di;
+    PGEOF_TRY(current_device_info(&di));
+    const unsigned blocks = (unsigned)std::min<uint64_t>(ceil_div_u(n, 256), (uint64_t)di->sm_count * 8);
+    pad_xyz_kernel<<<blocks, 256, 0, s>>>(xyz, n, out);
+    count_launch();
+    return check_launch("pad_xyz_kernel");
+}
+
+template <int S>
+static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
+    const size_t smem = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
+    const unsigned blocks = ceil_div_u(a.n_points, kFeatThreads);
+    features_kernel<S><<<blocks, kFeatThreads, smem, s>>>(a);
+    count_launch();
+    return check_launch("features_kernel");
+}
+
+int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                    uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
+                    float* out, unsigned long long* resolved, cudaStream_t s) {
+    if (n_points == 0) return PGEOF_OK;
+    FeatArgs a{};
+    a.xyz4 = xyz4;
+    a.n_xyz = (uint32_t)n_xyz;
+    a.nn = nn;
+    a.nnz = nnz;
+    a.ptr = ptr;
+    a.n_points = (uint32_t)n_points;
+    a.order = eig_order();
+    a.err = device_error_word();
+    a.resolved = resolved;
+    a.out = out;
+    if (full) {
+        a.full = 1;
+        a.k_min = (uint32_t)std::min<uint64_t>(k_min, 0xffffffffull);
+        a.n_scales = 1;
+        a.out_scales = 1;
+        a.scale_offset = 0;
+        return launch_features_s<1>(a, s);
+    }
+    a.full = 0;
+    a.out_scales = n_scales;
+    for (int s0 = 0; s0 < n_scales; s0 += kMaxScalesPerLaunch) {
+        const int cnt = std::min(kMaxScalesPerLaunch, n_scales - s0);
+        a.n_scales = cnt;
+        a.scale_offset = s0;
+        for (int q = 0; q < cnt; ++q) a.scales[q] = scales[s0 + q];
+        int st;
+        if (cnt == 1) st = launch_features_s<1>(a, s);
+        else if (cnt == 2) st = launch_features_s<2>(a, s);
+        else if (cnt <= 4) st = launch_features_s<4>(a, s);
+        else st = launch_features_s<8>(a, s);
+        if (st != PGEOF_OK) return st;
+    }
+    return PGEOF_OK;
+}
+
+int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                   uint64_t n_points, uint32_t k_min, uint32_t k_step, uint32_t k_min_search, float* out,
+                   unsigned long long* stats, cudaStream_t s) {
+    if (n_points == 0) return PGEOF_OK;
+    OptArgs a{};
+    a.xyz4 = xyz4;
+    a.n_xyz = (uint32_t)n_xyz;
+    a.nn = nn;
+    a.nnz = nnz;
+    a.ptr = ptr;
+    a.n_points = (uint32_t)n_points;
+    a.k_min = k_min;
+    a.k_step = k_step;
+    a.k_min_search = k_min_search;
+    a.order = eig_order();
+    a.out = out;
+    a.err = device_error_word();
+    a.stats = stats;
+    optimal_kernel<<<ceil_div_u(n_points, kOptThreads), kOptThreads, 0, s>>>(a);
+    count_launch();
+    return check_launch("optimal_kernel");
+}
+
+}  // namespace pgeof

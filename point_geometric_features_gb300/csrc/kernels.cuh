@@ -1,0 +1,84 @@
+// kernels.cuh -- host-side launchers shared between the translation units of
+// libpgeof_cuda (feature kernels, grid index, neighbour search).
+#pragma once
+
+#include "common.cuh"
+
+namespace pgeof {
+
+// ----------------------------------------------------------- feature passes
+int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s);
+int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                    uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
+                    float* out, unsigned long long* resolved, cudaStream_t s);
+int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                   uint64_t n_points, uint32_t k_min, uint32_t k_step, uint32_t k_min_search, float* out,
+                   unsigned long long* stats, cudaStream_t s);
+
+// ----------------------------------------------------------- grid index
+// Uniform grid over the bounding box. Cells are numbered x-fastest
+// (id = (cz * gy + cy) * gx + cx); points are counting-sorted by cell so every
+// cell, and every run of cells along x, is one contiguous range.
+struct GridParams {
+    float ox, oy, oz;  // origin (bounding-box minimum)
+    float h, inv_h;    // cell edge and its inverse
+    int gx, gy, gz;    // cells per axis
+    uint32_t n_cells;  // gx * gy * gz
+    float margin;      // slack added to every cell-distance bound
+};
+
+// A point in cell order: coordinates plus its original row index.
+template <typename T>
+struct SPoint;
+template <>
+struct __align__(16) SPoint<float> {
+    float x, y, z;
+    uint32_t idx;
+};
+template <>
+struct __align__(32) SPoint<double> {
+    double x, y, z;
+    uint32_t idx, pad;
+};
+
+template <typename T>
+struct GridIndex {
+    GridParams g{};
+    uint64_t n = 0;
+    uint32_t* cell_start = nullptr;  // n_cells + 1 (device)
+    SPoint<T>* pts = nullptr;        // n (device), cell order
+    Scratch cell_mem, pts_mem;
+};
+
+// Build the index of `xyz` (device, row-major (n, 3)). `k_target` steers the
+// cell size towards ~k_target/3.5 points per cell around an average point;
+// `h_min`/`h_max` (> 0) clamp the edge (radius searches).
+template <typename T>
+int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h_max, GridIndex<T>& out,
+               cudaStream_t s);
+
+// Counting-sort arbitrary query points into `grid`'s cell order.
+template <typename T>
+int sort_queries(const T* q, uint64_t m, const GridParams& g, Scratch& out_mem, SPoint<T>** out, cudaStream_t s);
+
+// ----------------------------------------------------------- neighbour search
+enum SearchMode { MODE_KNN = 0, MODE_RADIUS = 1 };
+
+template <typename T>
+struct SearchOut {
+    void* indices = nullptr;          // uint32 (knn) or int32 (radius), (m, k)
+    T* sqr_dist = nullptr;            // (m, k), may be null
+    uint32_t* found = nullptr;        // optional: uncapped count inside the radius
+    bool radius_fill_last = true;     // nanoflann RKNN: radius^2 in the last slot of short rows
+};
+
+template <typename T>
+int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, int mode, uint32_t k, T radius,
+                  const SearchOut<T>& out, cudaStream_t s);
+
+// PCA + selected features from a radius-search neighbour table (selected path).
+template <typename T>
+int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint32_t* found, uint32_t max_knn,
+                        const int32_t* ids, int n_ids, T* out, cudaStream_t s);
+
+}  // namespace pgeof
