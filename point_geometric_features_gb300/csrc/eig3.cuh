@@ -171,7 +171,52 @@ __device__ __noinline__ void pca_solve_f64(const Cov<T> cov, int order, Pca<T>* 
     finish_pca<T, double>(w, v, order, *out);
 }
 
-// Float covariance -> PCA. Counts the neighbourhoods re-solved in double.
+// ---- compensated ("double-float") arithmetic on the FP32 pipes: a value is
+// hi + lo with |lo| <= ulp(hi)/2 (Dekker 1971; Knuth TAOCP vol. 2, 4.2.2).
+struct DFloat {
+    float hi, lo;
+};
+__device__ __forceinline__ DFloat two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DFloat two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DFloat quick_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DFloat df_add(DFloat x, DFloat y) {
+    const DFloat s = two_sum(x.hi, y.hi);
+    return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ DFloat df_mul(DFloat x, float a) {
+    const DFloat p = two_prod(x.hi, a);
+    return quick_two_sum(p.hi, __fmaf_rn(x.lo, a, p.lo));
+}
+
+// Rayleigh quotient v^T A v / v^T v of the float covariance, evaluated in
+// double-float. With v accurate to angle t the result is within t^2 * gap of
+// the exact eigenvalue, and rounding contributes ~2^-46 |A| instead of the
+// ~2^-24 |A| of a plain float evaluation -- which is what a small eigenvalue
+// needs: the reference's formulas divide by sqrt(lambda_min) + 1e-3.
+__device__ __forceinline__ float rayleigh(const Cov<float>& c, float x, float y, float z) {
+    DFloat q = df_mul(two_prod(x, x), c.xx);
+    q = df_add(q, df_mul(two_prod(y, y), c.yy));
+    q = df_add(q, df_mul(two_prod(z, z), c.zz));
+    q = df_add(q, df_mul(two_prod(x, y), __fmul_rn(2.0f, c.xy)));
+    q = df_add(q, df_mul(two_prod(x, z), __fmul_rn(2.0f, c.xz)));
+    q = df_add(q, df_mul(two_prod(y, z), __fmul_rn(2.0f, c.yz)));
+    DFloat n = two_prod(x, x);
+    n = df_add(n, two_prod(y, y));
+    n = df_add(n, two_prod(z, z));
+    return __fdiv_rn(__fadd_rn(q.hi, q.lo), __fadd_rn(n.hi, n.lo));
+}
+
+// Float covariance -> PCA. `resolved` reports a re-solve in double.
 __device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, Pca<float>& out, bool& resolved) {
     float a[3][3], v[3][3], w[3];
     load_cov(cov, a);
@@ -188,6 +233,11 @@ __device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, 
         resolved = true;
         pca_solve_f64<float>(cov, order, &out);
         return;
+    }
+    if (sweeps > 0) {
+        // eigenvalues to ~1e-14 |A| from the well-conditioned eigenvectors
+#pragma unroll
+        for (int i = 0; i < 3; ++i) w[i] = rayleigh(cov, v[0][i], v[1][i], v[2][i]);
     }
     finish_pca<float, float>(w, v, order, out);
 }

@@ -1,0 +1,169 @@
+"""GPU neighbour search parity (include/nn_search.hpp:31-132) against the
+oracle and scipy, through the drop-in Python API (pgeof_ext -> C ABI)."""
+
+import numpy as np
+import pytest
+from scipy.spatial import KDTree
+
+from oracle import oracle
+from point_geometric_features_gb300.synthetic import outdoor_scene, uniform_cube
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_test_knn(cuda, pgeof, golden):
+    """tests/test_pgeof.py:8-15 with the committed seeded fixture."""
+    g = golden("knn_1000_k10.npz")
+    idx, d2 = pgeof.knn_search(g["xyz"], g["xyz"], 10)
+    assert idx.dtype == np.uint32 and d2.dtype == np.float32 and idx.shape == (1000, 10)
+    np.testing.assert_equal(idx.astype(np.int64), g["scipy_idx"])
+
+
+def test_reference_test_radius(cuda, pgeof, golden):
+    """tests/test_pgeof.py:18-27 with the committed seeded fixture."""
+    g = golden("radius_1000_r02_k10.npz")
+    idx, d2 = pgeof.radius_search(g["xyz"], g["xyz"], 0.2, 10)
+    assert idx.dtype == np.int32 and idx.shape == (1000, 10)
+    np.testing.assert_equal(idx.astype(np.int64), g["scipy_idx"])
+
+
+@pytest.mark.parametrize("k", [1, 2, 7, 20, 50, 64, 100])
+def test_knn_exact_uniform(cuda, pgeof, k):
+    xyz = uniform_cube(10_000, seed=k)
+    idx, d2 = pgeof.knn_search(xyz, xyz, k)
+    ri, rd = oracle.knn_search(xyz, xyz, k)
+    np.testing.assert_array_equal(d2, rd)  # bit-identical float distances
+    np.testing.assert_array_equal(idx, ri)
+
+
+def test_knn_exact_scene(cuda, pgeof):
+    xyz = outdoor_scene(40_000, seed=1)
+    idx, d2 = pgeof.knn_search(xyz, xyz, 50)
+    ri, rd = oracle.knn_search(xyz, xyz, 50)
+    np.testing.assert_array_equal(d2, rd)
+    np.testing.assert_array_equal(idx, ri)
+
+
+def test_knn_separate_queries_outside_box(cuda, pgeof):
+    rng = np.random.default_rng(3)
+    data = rng.random((5000, 3), dtype=np.float32)
+    query = (rng.random((777, 3), dtype=np.float32) * 3.0 - 1.0).astype(np.float32)  # many outside the data box
+    idx, d2 = pgeof.knn_search(data, query, 12)
+    ri, rd = oracle.knn_search(data, query, 12)
+    np.testing.assert_array_equal(d2, rd)
+    np.testing.assert_array_equal(idx, ri)
+
+
+def test_knn_k_equals_n(cuda, pgeof):
+    xyz = uniform_cube(300, seed=4)
+    idx, d2 = pgeof.knn_search(xyz, xyz, 300)
+    ri, rd = oracle.knn_search(xyz, xyz, 300)
+    np.testing.assert_array_equal(idx, ri)
+    np.testing.assert_array_equal(d2, rd)
+
+
+def test_knn_duplicates_ties_by_index(cuda, pgeof):
+    """Many exact duplicates force the refinement passes (equal distances are
+    ordered by index)."""
+    rng = np.random.default_rng(5)
+    base = rng.random((200, 3), dtype=np.float32)
+    xyz = np.concatenate([base, np.repeat(base[:3], 400, axis=0), rng.random((2000, 3), dtype=np.float32)])
+    xyz = np.ascontiguousarray(xyz.astype(np.float32))
+    for k in (5, 64, 450):
+        idx, d2 = pgeof.knn_search(xyz, xyz, k)
+        ri, rd = oracle.knn_search(xyz, xyz, k)
+        np.testing.assert_array_equal(d2, rd)
+        np.testing.assert_array_equal(idx, ri)
+
+
+def test_knn_planar_and_single_axis(cuda, pgeof):
+    rng = np.random.default_rng(6)
+    plane = rng.random((4000, 3), dtype=np.float32)
+    plane[:, 2] = 0.0
+    line = np.zeros((1000, 3), np.float32)
+    line[:, 0] = rng.random(1000, dtype=np.float32)
+    for xyz in (plane, line):
+        idx, d2 = pgeof.knn_search(xyz, xyz, 16)
+        ri, rd = oracle.knn_search(xyz, xyz, 16)
+        np.testing.assert_array_equal(d2, rd)
+        np.testing.assert_array_equal(idx, ri)
+
+
+def test_knn_errors_and_empty(cuda, pgeof):
+    xyz = uniform_cube(10, seed=1)
+    with pytest.raises(ValueError):
+        pgeof.knn_search(xyz, xyz, 11)
+    with pytest.raises(TypeError):
+        pgeof.knn_search(xyz.astype(np.float64), xyz, 2)
+    idx, d2 = pgeof.knn_search(xyz, np.zeros((0, 3), np.float32), 3)
+    assert idx.shape == (0, 3)
+    idx, d2 = pgeof.knn_search(xyz, xyz, 0)
+    assert idx.shape == (10, 0)
+    one = np.array([[0.5, 0.5, 0.5]], np.float32)
+    idx, d2 = pgeof.knn_search(one, one, 1)
+    assert idx[0, 0] == 0 and d2[0, 0] == 0
+
+
+@pytest.mark.parametrize("r,k", [(0.05, 30), (0.1, 16), (0.02, 64), (0.3, 8)])
+def test_radius_exact(cuda, pgeof, r, k):
+    xyz = uniform_cube(8000, seed=int(r * 1000))
+    idx, d2 = pgeof.radius_search(xyz, xyz, r, k)
+    ri, rd = oracle.radius_search(xyz, xyz, r, k)
+    np.testing.assert_array_equal(idx, ri)
+    np.testing.assert_array_equal(d2, rd)  # includes nanoflann's r^2 in the last slot of short rows
+
+
+def test_radius_scene_and_queries(cuda, pgeof):
+    data = outdoor_scene(30_000, seed=2)
+    rng = np.random.default_rng(2)
+    query = data[rng.choice(data.shape[0], 3000, replace=False)] + rng.normal(0, 0.3, (3000, 3)).astype(np.float32)
+    query = np.ascontiguousarray(query.astype(np.float32))
+    idx, d2 = pgeof.radius_search(data, query, 0.5, 64)
+    ri, rd = oracle.radius_search(data, query, 0.5, 64)
+    np.testing.assert_array_equal(idx, ri)
+    np.testing.assert_array_equal(d2, rd)
+
+
+def test_radius_errors(cuda, pgeof):
+    xyz = uniform_cube(10, seed=1)
+    with pytest.raises(ValueError):
+        pgeof.radius_search(xyz, xyz, 0.1, 11)
+    idx, d2 = pgeof.radius_search(xyz, xyz, 0.1, 0)
+    assert idx.shape == (10, 0)
+
+
+def test_knn_matches_scipy_large(cuda, pgeof):
+    """bench_knn.py shapes at 200k points: identical to scipy except at exact ties."""
+    rng = np.random.default_rng(21)
+    xyz = rng.uniform(0.0, 200.0, size=(200_000, 3)).astype(np.float32)
+    idx, _ = pgeof.knn_search(xyz, xyz, 50)
+    _, ref = KDTree(xyz).query(xyz[:5000], k=50, workers=-1)
+    mism = (idx[:5000].astype(np.int64) != ref).any(axis=1).mean()
+    assert mism < 1e-3, mism
+
+
+def test_knn_full_size_properties(cuda, pgeof):
+    """1M-point outdoor scene, k=50: sorted rows, self first, distances that
+    recompute exactly from the returned indices, and a 2000-query spot check
+    against the oracle's brute force."""
+    xyz = outdoor_scene(1_000_000, seed=1)
+    idx, d2 = pgeof.knn_search(xyz, xyz, 50)
+    assert np.all(np.diff(d2, axis=1) >= 0)
+    assert np.all(d2[:, 0] == 0)
+    rng = np.random.default_rng(0)
+    rows = rng.choice(xyz.shape[0], 2000, replace=False)
+    diff = (xyz[rows][:, None, :] - xyz[idx[rows]]).astype(np.float32)
+    rec = (diff[..., 0] * diff[..., 0] + diff[..., 1] * diff[..., 1]).astype(np.float32)
+    rec = (rec + diff[..., 2] * diff[..., 2]).astype(np.float32)
+    np.testing.assert_array_equal(rec, d2[rows])
+    ri, rd = oracle.knn_search(xyz, xyz[rows], 50)
+    np.testing.assert_array_equal(d2[rows], rd)
+    np.testing.assert_array_equal(idx[rows], ri)
+
+
+def test_knn_deterministic(cuda, pgeof):
+    xyz = outdoor_scene(50_000, seed=9)
+    a = pgeof.knn_search(xyz, xyz, 32)
+    b = pgeof.knn_search(xyz, xyz, 32)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
