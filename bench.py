@@ -1,0 +1,408 @@
+"""Benchmark: points/s of kNN + multiscale features on a 1M-point outdoor scene.
+
+Workload (one step): the 1,000,000-point synthetic outdoor scene (100 x 100 x
+20 m; ground / walls / cylinders / scatter, seed 1) -> knn_search(k=50) ->
+CSR (nn = indices, nn_ptr = 50 * arange) -> compute_features_multiscale with
+k_scales = [10, 20, 50]. This is pgeof's documented pipeline (README.md:125-144
+of the reference) on the workload its kNN+features metric is quoted on.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Arms:
+  ours       device-resident inputs through the drop-in API (torch CUDA
+             tensors in, CUDA tensors out) -> `value`; the same pipeline through
+             the numpy API with host buffers (copies inside) -> `e2e`.
+  reference  the reference's CPU path timed on this host's cores. The reference
+             cannot be built here (its Eigen / nanoflann / Taskflow submodules
+             are empty), so its stand-in runs: scipy's cKDTree for the kNN
+             stage (the reference's own bench comparator, tests/bench_knn.py) and
+             the threaded C restatement of include/pca.hpp for the features.
+
+N > 1 (torchrun): every rank runs the same per-GPU workload on its own cloud
+(seed 1 + rank) -- replicas, weak scaling, no collective on the data path.
+Printed by rank 0: one JSON line.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_POINTS = 1_000_000
+K = 50
+SCALES = [10, 20, 50]
+METRIC = "points/s kNN+features, 1M pts k=50 (batched vs plain GPU); serving p50/p99 ms"
+UNIT = "points/s"
+WORKLOAD = "1M-point outdoor scene, knn_search k=50 -> compute_features_multiscale [10,20,50]"
+
+# algorithmic (compulsory) HBM bytes per point of each kernel on this workload
+ALGO_BYTES_PER_POINT = {
+    "knn_search_kernel": 12 + 12 + 8 * K,  # query + data + (uint32 index, float distance) x k
+    "features_kernel": 4 * K + 4 + 12 + 44 * len(SCALES),  # nn + nn_ptr + own xyz + 11 floats per scale
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "knn_search_kernel_1M_k50.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch_full_size:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled every 100 ms."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        return self.summary()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in self.rows if num(r[0]) is not None]
+        smax = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        loaded = [v for v in sm if smax and v >= 0.5 * max(smax)] or sm
+        return {"sm_mhz": float(np.median(loaded)) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args, rank, world, local):
+    import torch
+
+    import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    xyz = outdoor_scene(N_POINTS, seed=1 + rank)
+    t = torch.from_numpy(xyz).to(dev)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    def step():
+        idx, _d2 = pgeof.knn_search(t, t, K)
+        nn = idx.view(-1)
+        nn_ptr = torch.arange(0, K * (N_POINTS + 1), K, dtype=torch.int32, device=dev)
+        return pgeof.compute_features_multiscale(t, nn, nn_ptr, SCALES, check=False)
+
+    for _ in range(max(args.warmup, 3)):
+        out = step()
+    pgeof.check_device_errors()
+    torch.cuda.synchronize()
+    barrier()
+
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    smi_index = int(vis.split(",")[local]) if vis and vis.split(",")[local].strip().isdigit() else local
+    clocks = ClockSampler(smi_index)
+    clocks.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = pgeof.kernel_launch_count()
+    pgeof.profile_kernels(True)
+    pgeof.kernel_profile()  # clear
+    torch.cuda.synchronize()
+    barrier()
+    for i in range(args.steps):
+        flush.zero_()  # evict the 12 MB cloud from L2 between steps (outside the events)
+        starts[i].record()
+        out = step()
+        stops[i].record()
+    torch.cuda.synchronize()
+    barrier()
+    prof = pgeof.kernel_profile()
+    pgeof.profile_kernels(False)
+    launches = pgeof.kernel_launch_count() - launches0
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, stops))
+    total_ms = ms
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    pgeof.check_device_errors()
+    assert out.shape == (N_POINTS, len(SCALES), 11) and bool(torch.isfinite(out).all())
+
+    # e2e: the numpy drop-in API, host buffers in and out
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    nn_ptr_h = (np.arange(N_POINTS + 1, dtype=np.int64) * K).astype(np.uint32)
+
+    def e2e_step():
+        idx, _d2 = pgeof.knn_search(xyz, xyz, K)
+        return pgeof.compute_features_multiscale(xyz, idx.reshape(-1), nn_ptr_h, SCALES)
+
+    if args.skip_e2e:
+        e2e_steps = 0
+        res = out.cpu().numpy()
+        e2e_s = float("nan")
+    else:
+        e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            res = e2e_step()
+        e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    clk = clocks.stop()
+    assert res.shape == (N_POINTS, len(SCALES), 11)
+    h2d = xyz.nbytes + xyz.nbytes + N_POINTS * K * 4 + (N_POINTS + 1) * 4
+    d2h = N_POINTS * K * 8 + N_POINTS * len(SCALES) * 11 * 4
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return None
+
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    for name, (n, kms) in prof.items():
+        kernels[name] = {"launches": n, "total_ms": round(kms, 4), "share": round(kms / max(ms, 1e-9), 4)}
+    dom = max(prof.items(), key=lambda kv: kv[1][1])[0] if prof else None
+    roofline = None
+    if dom:
+        n, kms = prof[dom]
+        per_launch_s = kms / n / 1e3
+        algo = ALGO_BYTES_PER_POINT.get(dom)
+        if algo:
+            achieved = algo * N_POINTS / per_launch_s / 1e9
+            roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                        "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                        "algorithmic_bytes_per_launch": algo * N_POINTS,
+                        "avg_launch_ms": round(kms / n, 4),
+                        "traffic": traffic_from_profile()}
+    value = world * N_POINTS * args.steps / (total_ms / 1e3)
+    line = {
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded outdoor scene; the reference publishes no dataset or numbers)",
+        "config": {"workload": WORKLOAD, "points_per_gpu": N_POINTS, "k": K, "k_scales": SCALES,
+                   "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(world * N_POINTS * e2e_steps / e2e_s, 1) if e2e_steps else None, "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "path": "numpy drop-in API (pageable host arrays)", "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": roofline,
+        "kernels": kernels,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(sample=200_000)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return line
+
+
+# ---------------------------------------------------------------- CPU stand-in
+def cpu_pipeline(xyz, sample_rows, threads):
+    """The reference's CPU pipeline stand-in: cKDTree build over the full cloud
+    (the reference rebuilds its KD-tree on every call), then kNN (k=50) for
+    `sample_rows` and the threaded C restatement of the multiscale feature pass
+    on those rows. Returns (build seconds, per-sample seconds)."""
+    from scipy.spatial import cKDTree
+
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    tree = cKDTree(xyz)
+    t1 = time.perf_counter()
+    _, idx = tree.query(xyz[sample_rows], k=K, workers=threads)
+    nn = idx.reshape(-1).astype(np.uint32)
+    nn_ptr = (np.arange(sample_rows.size + 1, dtype=np.int64) * K).astype(np.uint32)
+    oracle.compute_features_multiscale(xyz, nn, nn_ptr, SCALES, threads=threads)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
+
+
+def projected_rate(build_s, sample_s, sample):
+    """points/s of a full 1M-point call: one tree build + every query."""
+    return N_POINTS / (build_s + sample_s * N_POINTS / sample)
+
+
+def cpu_baseline(sample):
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    xyz = outdoor_scene(N_POINTS, seed=1)
+    rows = np.random.default_rng(0).choice(N_POINTS, sample, replace=False)
+    cores = os.cpu_count() or 1
+    build_s, sample_s = cpu_pipeline(xyz, rows, cores)
+    return {"value": round(projected_rate(build_s, sample_s, sample), 1), "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": f"cKDTree build over all 1M points ({build_s:.2f} s) + kNN k=50 and multiscale features for "
+                      f"{sample} random query points ({sample_s:.2f} s), projected to one full 1M-point call; "
+                      f"{cores} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    xyz = outdoor_scene(N_POINTS, seed=1)
+    cores = os.cpu_count() or 1
+    sample = 50_000
+    rng = np.random.default_rng(0)
+    for _ in range(max(args.warmup, 1)):
+        cpu_pipeline(xyz, rng.choice(N_POINTS, sample, replace=False), cores)
+    build = samp = 0.0
+    for _ in range(args.steps):
+        b, t = cpu_pipeline(xyz, rng.choice(N_POINTS, sample, replace=False), cores)
+        build += b
+        samp += t
+    value = projected_rate(build / args.steps, samp / args.steps, sample)
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": UNIT,
+        "n_gpus": 0,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 1),
+        "ms_per_step": round(N_POINTS / value * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded outdoor scene)",
+        "config": {"workload": WORKLOAD, "points_per_step": N_POINTS},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"per step: cKDTree build over all 1M points + kNN k=50 and multiscale features "
+                                   f"for {sample} random query points, projected to one full 1M-point call"},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "pgeof cannot be built here (empty Eigen/nanoflann/Taskflow submodules, no nanobind); "
+                "the CPU stand-in above is timed instead",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

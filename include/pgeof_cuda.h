@@ -83,6 +83,13 @@ uint64_t pgeof_kernel_launch_count(void);
  * v2 is the surface normal). Process-wide. */
 int pgeof_set_eig_order(int order);
 int pgeof_get_eig_order(void);
+/* Kernel timing for measurement harnesses (no reference counterpart). While
+ * enabled, every kernel launch is bracketed by CUDA events recorded on the
+ * stream it is launched on. pgeof_profile_report() waits for those events,
+ * writes one line "<kernel> <launches> <total_ms>\n" per kernel name into buf
+ * (NUL-terminated, truncated to buf_len) and clears the record. */
+int pgeof_profile_enable(int on);
+int pgeof_profile_report(char* buf, size_t buf_len);
 /* Synchronises `stream` and returns (then clears) the device-side data-error
  * bits recorded since the last call (bit 0: nn index out of range, bit 1:
  * nn_ptr not monotone or beyond len(nn), bit 2: internal bound exceeded). */

@@ -71,6 +71,20 @@ def kernel_launch_count() -> int:
     return int(_ext._launch_count())
 
 
+def profile_kernels(enabled: bool) -> None:
+    """Bracket every kernel launch with CUDA events on its own stream."""
+    _ext._profile_enable(bool(enabled))
+
+
+def kernel_profile() -> dict:
+    """{kernel name: (launches, total ms)} since the last call (waits for the events)."""
+    out = {}
+    for line in _ext._profile_report().splitlines():
+        name, n, ms = line.split()
+        out[name] = (int(n), float(ms))
+    return out
+
+
 def check_device_errors(stream=None) -> None:
     """Synchronise ``stream`` (torch stream, int handle or None = current torch
     stream) and raise ValueError if a device call saw invalid CSR input."""

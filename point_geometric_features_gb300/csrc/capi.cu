@@ -230,6 +230,51 @@ int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const in
 
 }  // namespace
 
+// ------------------------------------------------------------ kernel timing
+std::atomic<int> g_profile_on{0};
+namespace {
+struct TimedLaunch {
+    const char* name;
+    cudaEvent_t a, b;
+};
+std::mutex g_prof_mu;
+std::vector<TimedLaunch> g_prof;
+std::vector<cudaEvent_t> g_event_pool;
+
+cudaEvent_t take_event() {
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        if (!g_event_pool.empty()) {
+            cudaEvent_t e = g_event_pool.back();
+            g_event_pool.pop_back();
+            return e;
+        }
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+}  // namespace
+
+KernelTimer::KernelTimer(const char* kernel_name, cudaStream_t stream) : name(kernel_name), s(stream) {
+    if (g_profile_on.load(std::memory_order_relaxed)) {
+        a = take_event();
+        if (a) cudaEventRecord(a, s);
+    }
+}
+
+KernelTimer::~KernelTimer() {
+    if (!a) return;
+    cudaEvent_t b = take_event();
+    if (!b) return;
+    cudaEventRecord(b, s);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof.push_back({name, a, b});
+}
+
 void set_error(const std::string& msg) { t_last_error = msg; }
 int fail(int status, const std::string& msg) {
     t_last_error = msg;
@@ -314,6 +359,62 @@ int pgeof_set_eig_order(int order) {
     return PGEOF_OK;
 }
 int pgeof_get_eig_order(void) { return g_eig_order.load(); }
+
+int pgeof_profile_enable(int on) {
+    g_profile_on.store(on ? 1 : 0);
+    return PGEOF_OK;
+}
+
+int pgeof_profile_report(char* buf, size_t buf_len) {
+    std::vector<TimedLaunch> rec;
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        rec.swap(g_prof);
+    }
+    struct Agg {
+        std::string name;
+        uint64_t n = 0;
+        double ms = 0.0;
+    };
+    std::vector<Agg> agg;
+    int status = PGEOF_OK;
+    for (const TimedLaunch& t : rec) {
+        float ms = 0.0f;
+        cudaError_t e = cudaEventSynchronize(t.b);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, t.a, t.b);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            status = fail(PGEOF_ERR_CUDA, std::string("kernel timing: ") + cudaGetErrorString(e));
+            continue;
+        }
+        auto it = std::find_if(agg.begin(), agg.end(), [&](const Agg& x) { return x.name == t.name; });
+        if (it == agg.end()) {
+            agg.push_back({t.name, 0, 0.0});
+            it = agg.end() - 1;
+        }
+        it->n += 1;
+        it->ms += ms;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        for (const TimedLaunch& t : rec) {
+            g_event_pool.push_back(t.a);
+            g_event_pool.push_back(t.b);
+        }
+    }
+    std::string out;
+    for (const Agg& x : agg) {
+        char line[256];
+        snprintf(line, sizeof(line), "%s %llu %.6f\n", x.name.c_str(), (unsigned long long)x.n, x.ms);
+        out += line;
+    }
+    if (buf && buf_len) {
+        const size_t n = std::min(out.size(), buf_len - 1);
+        memcpy(buf, out.data(), n);
+        buf[n] = '\0';
+    }
+    return status;
+}
 
 int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits) {
     DevState* st;

@@ -49,6 +49,19 @@ extern std::atomic<uint64_t> g_launch_count;
 inline void count_launch(uint64_t n = 1) { g_launch_count.fetch_add(n, std::memory_order_relaxed); }
 int check_launch(const char* what);  // cudaGetLastError after a launch
 
+// Brackets the kernel launches of its scope with CUDA events on `s` while
+// kernel timing is enabled (pgeof_profile_enable); a no-op otherwise.
+extern std::atomic<int> g_profile_on;
+struct KernelTimer {
+    const char* name;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    KernelTimer(const char* kernel_name, cudaStream_t stream);
+    ~KernelTimer();
+    KernelTimer(const KernelTimer&) = delete;
+    KernelTimer& operator=(const KernelTimer&) = delete;
+};
+
 // ----------------------------------------------------------------- device info
 struct DeviceInfo {
     int device = -1;

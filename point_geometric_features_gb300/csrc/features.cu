@@ -430,6 +430,7 @@ int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     const unsigned blocks = (unsigned)std::min<uint64_t>(ceil_div_u(n, 256), (uint64_t)di->sm_count * 8);
+    KernelTimer kt("pad_xyz_kernel", s);
     pad_xyz_kernel<<<blocks, 256, 0, s>>>(xyz, n, out);
     count_launch();
     return check_launch("pad_xyz_kernel");
@@ -439,6 +440,7 @@ template <int S>
 static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
     const size_t smem = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
     const unsigned blocks = ceil_div_u(a.n_points, kFeatThreads);
+    KernelTimer kt("features_kernel", s);
     features_kernel<S><<<blocks, kFeatThreads, smem, s>>>(a);
     count_launch();
     return check_launch("features_kernel");
@@ -502,6 +504,7 @@ int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint6
     a.out = out;
     a.err = device_error_word();
     a.stats = stats;
+    KernelTimer kt("optimal_kernel", s);
     optimal_kernel<<<ceil_div_u(n_points, kOptThreads), kOptThreads, 0, s>>>(a);
     count_launch();
     return check_launch("optimal_kernel");

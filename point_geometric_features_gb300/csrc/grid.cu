@@ -200,6 +200,7 @@ int exclusive_scan(const uint32_t* in, uint32_t G, uint32_t* out, cudaStream_t s
     const uint32_t nb = ceil_div_u(G, kScanTile);
     Scratch part;
     PGEOF_TRY(part.alloc((size_t)nb * sizeof(uint32_t), s));
+    KernelTimer kt("scan_kernels", s);
     scan_partials_kernel<<<nb, kScanThreads, 0, s>>>(in, G, part.as<uint32_t>());
     scan_top_kernel<<<1, kScanThreads, 0, s>>>(part.as<uint32_t>(), nb);
     scan_final_kernel<<<nb, kScanThreads, 0, s>>>(in, G, part.as<uint32_t>(), out);
@@ -246,6 +247,7 @@ static int occupancy(const T* xyz, uint64_t n, const GridParams& g, uint32_t* co
                      double& m_w, cudaStream_t s) {
     PGEOF_CUDA_TRY(cudaMemsetAsync(counts, 0, (size_t)g.n_cells * sizeof(uint32_t), s));
     PGEOF_CUDA_TRY(cudaMemsetAsync(dsum, 0, sizeof(unsigned long long), s));
+    KernelTimer kt("grid_occupancy_kernels", s);
     hist_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, g, counts, nullptr, nullptr);
     sumsq_kernel<<<grid_blocks(g.n_cells, 256), 256, 0, s>>>(counts, g.n_cells, dsum);
     count_launch(2);
@@ -271,7 +273,10 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
     uint32_t* box = misc.as<uint32_t>();
     PGEOF_CUDA_TRY(cudaMemsetAsync(box, 0xff, 3 * sizeof(uint32_t), s));
     PGEOF_CUDA_TRY(cudaMemsetAsync(box + 3, 0, 3 * sizeof(uint32_t), s));
-    bbox_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, box);
+    {
+        KernelTimer kt("bbox_kernel", s);
+        bbox_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, box);
+    }
     count_launch();
     PGEOF_TRY(check_launch("bbox_kernel"));
     uint32_t hb[6];
@@ -341,11 +346,15 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
     PGEOF_TRY(cell.alloc((size_t)n * sizeof(uint32_t), s));
     PGEOF_TRY(rank.alloc((size_t)n * sizeof(uint32_t), s));
     PGEOF_CUDA_TRY(cudaMemsetAsync(counts.p, 0, (size_t)g.n_cells * sizeof(uint32_t), s));
-    hist_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, g, counts.as<uint32_t>(), cell.as<uint32_t>(),
-                                                        rank.as<uint32_t>());
+    {
+        KernelTimer kt("hist_kernel", s);
+        hist_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, g, counts.as<uint32_t>(), cell.as<uint32_t>(),
+                                                            rank.as<uint32_t>());
+    }
     count_launch();
     PGEOF_TRY(check_launch("hist_kernel"));
     PGEOF_TRY(exclusive_scan(counts.as<uint32_t>(), g.n_cells, out.cell_start, s));
+    KernelTimer kt("scatter_kernel", s);
     scatter_kernel<T><<<grid_blocks(n, 256), 256, 0, s>>>(xyz, n, out.cell_start, cell.as<uint32_t>(),
                                                            rank.as<uint32_t>(), out.pts);
     count_launch();
@@ -363,11 +372,15 @@ int sort_queries(const T* q, uint64_t m, const GridParams& g, Scratch& out_mem, 
     PGEOF_TRY(cell.alloc((size_t)m * sizeof(uint32_t), s));
     PGEOF_TRY(rank.alloc((size_t)m * sizeof(uint32_t), s));
     PGEOF_CUDA_TRY(cudaMemsetAsync(counts.p, 0, (size_t)g.n_cells * sizeof(uint32_t), s));
-    hist_kernel<T><<<grid_blocks(m, 256), 256, 0, s>>>(q, m, g, counts.as<uint32_t>(), cell.as<uint32_t>(),
-                                                        rank.as<uint32_t>());
+    {
+        KernelTimer kt("query_hist_kernel", s);
+        hist_kernel<T><<<grid_blocks(m, 256), 256, 0, s>>>(q, m, g, counts.as<uint32_t>(), cell.as<uint32_t>(),
+                                                            rank.as<uint32_t>());
+    }
     count_launch();
     PGEOF_TRY(check_launch("hist_kernel(queries)"));
     PGEOF_TRY(exclusive_scan(counts.as<uint32_t>(), g.n_cells, start.as<uint32_t>(), s));
+    KernelTimer kt("query_scatter_kernel", s);
     scatter_kernel<T><<<grid_blocks(m, 256), 256, 0, s>>>(q, m, start.as<uint32_t>(), cell.as<uint32_t>(),
                                                            rank.as<uint32_t>(), out_mem.as<SPoint<T>>());
     count_launch();

@@ -21,6 +21,7 @@
 #include <pybind11/stl.h>
 
 #include <cstdint>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -245,6 +246,18 @@ PYBIND11_MODULE(pgeof_ext, m) {
     m.def("_launch_count", []() { return (uint64_t)pgeof_kernel_launch_count(); });
     m.def("_set_eig_order", [](int order) { check(pgeof_set_eig_order(order)); });
     m.def("_get_eig_order", &pgeof_get_eig_order);
+    m.def("_profile_enable", [](bool on) { check(pgeof_profile_enable(on ? 1 : 0)); });
+    m.def("_profile_report", []() {
+        std::string buf(1 << 16, '\0');
+        int st;
+        {
+            py::gil_scoped_release nogil;
+            st = pgeof_profile_report(&buf[0], buf.size());
+        }
+        check(st);
+        buf.resize(strlen(buf.c_str()));
+        return buf;
+    });
     m.def("_take_device_errors", [](uintptr_t stream) {
         uint32_t bits = 0;
         int st;

@@ -607,6 +607,7 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m
     a.out_found = out.found;
     a.fill_last = out.radius_fill_last ? 1 : 0;
     a.err = device_error_word();
+    KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
     kern<<<(unsigned)blocks, kSearchWarps * 32, smem, s>>>(a);
     count_launch();
     return check_launch("search_kernel");
@@ -629,6 +630,7 @@ int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint
         a.n_ids = std::min(kSelIdsPerLaunch, n_ids - off);
         a.id_offset = off;
         for (int t = 0; t < a.n_ids; ++t) a.ids[t] = ids[off + t];
+        KernelTimer kt("selected_pca_kernel", s);
         selected_pca_kernel<T><<<ceil_div_u(n, kSelThreads), kSelThreads, 0, s>>>(a);
         count_launch();
         PGEOF_TRY(check_launch("selected_pca_kernel"));
