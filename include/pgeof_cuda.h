@@ -151,6 +151,23 @@ int pgeof_compute_features_selected_f64(const double* xyz, int64_t n, double sea
                                         const int32_t* selected, int64_t n_selected, double* features,
                                         pgeof_stream_t stream);
 
+/* compute_features for callers that cannot allocate GPU memory. No
+ * counterpart in the reference: pgeof allocates freely on the CPU.
+ * Same arguments, checks and output as pgeof_compute_features_f32, plus
+ * `error_bits`: an optional caller-owned device word (zero it first) into
+ * which the kernels OR the data-error bits of pgeof_take_device_errors; with
+ * NULL they go to a library word that each call clears and no one reads.
+ * This call makes no cudaMalloc, cudaFree or pool allocation: its scratch (a
+ * float4 copy of xyz) is a fixed 16 MiB device array that every GPU loading
+ * the library holds until exit, so xyz is limited to 1,048,576 points (more
+ * returns PGEOF_ERR_INVALID_ARGUMENT). All calls share that array: calls that
+ * overlap on the GPU race and must be serialised by the caller. The first call
+ * on each device looks the array's address up (cudaGetSymbolAddress) with that
+ * device current; make it before any stream capture. */
+int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                       const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features,
+                                       uint32_t* error_bits, pgeof_stream_t stream);
+
 /* ------------------------------------------------ host-pointer API (sync) */
 /* Same semantics as the device entry points above; every pointer is host
  * memory. These are what the Python drop-in binding calls for numpy inputs. */

@@ -9,6 +9,10 @@
 // keeps one accumulator set per scale and fills every scale prefix in the same
 // two sweeps (the reference re-gathers each prefix). Output rows are staged in
 // shared memory and leave the block as one coalesced slab.
+#include <algorithm>
+#include <mutex>
+#include <string>
+
 #include "eig3.cuh"
 #include "kernels.cuh"
 
@@ -511,3 +515,108 @@ int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint6
 }
 
 }  // namespace pgeof
+
+// ===========================================================================
+// compute_features without any allocation (pgeof_compute_features_f32_noalloc)
+//
+// Some callers cannot allocate GPU memory while they call us: code running
+// under a fixed device-memory budget that was reserved up front (a serving
+// process that pre-sizes every buffer so it can never fail mid-request), hosts
+// whose own allocator owns the device heap and forbids foreign cudaMalloc /
+// pool traffic, and real-time loops where an allocation's latency or
+// implicit synchronisation is not acceptable. For them this entry point
+// keeps its only scratch -- the float4-padded copy of xyz that the feature
+// kernel gathers from -- in the fixed array below instead of in freshly
+// allocated memory. The caller still owns and passes every input and output.
+//
+// The array is file-scope device memory: every GPU that loads this library
+// holds it (16 MiB) until the process exits, and every call shares it. Calls
+// that overlap on the GPU (two streams, or two host threads) race on it and
+// must be serialised by the caller. Host code only ever sees a host-side
+// stand-in for the array's name, so the device address is fetched with
+// cudaGetSymbolAddress on the first call on each device, with that device
+// current; make that first call before any stream capture.
+// ===========================================================================
+static __device__ __align__(256) float4 g_noalloc_xyz4[1u << 20];
+static __device__ __align__(256) uint32_t g_noalloc_err[64];
+
+namespace pgeof {
+namespace {
+
+constexpr uint64_t kNoAllocMaxPoints = 1u << 20;  // capacity of g_noalloc_xyz4, in points
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocSetup {
+    std::once_flag once;
+    cudaError_t status = cudaSuccess;
+    float4* xyz4 = nullptr;   // device address of g_noalloc_xyz4
+    uint32_t* err = nullptr;  // device address of g_noalloc_err
+};
+NoAllocSetup g_noalloc_setup[kNoAllocMaxDevices];
+
+void noalloc_setup(NoAllocSetup& st) {
+    st.status = cudaGetSymbolAddress((void**)&st.xyz4, g_noalloc_xyz4);
+    if (st.status == cudaSuccess) st.status = cudaGetSymbolAddress((void**)&st.err, g_noalloc_err);
+}
+
+}  // namespace
+}  // namespace pgeof
+
+extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                                  const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min,
+                                                  float* features, uint32_t* error_bits, pgeof_stream_t stream) {
+    using namespace pgeof;
+    // the same argument checks as pgeof_compute_features_f32, then the capacity
+    if (k_min < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min should be > 1");
+    if (n_xyz < 0 || nnz < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "negative size");
+    if (n_points < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn_ptr must hold at least one entry");
+    if ((uint64_t)n_xyz > kNoAllocMaxPoints)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT,
+                    "xyz has " + std::to_string(n_xyz) + " points; pgeof_compute_features_f32_noalloc holds at most " +
+                        std::to_string(kNoAllocMaxPoints) + " (use pgeof_compute_features_f32)");
+    if ((uint64_t)n_points > 0xfffffffeull) return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn_ptr is too long");
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        (void)cudaGetLastError();
+        return fail(PGEOF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    NoAllocSetup& st = g_noalloc_setup[dev];
+    std::call_once(st.once, noalloc_setup, std::ref(st));
+    if (st.status != cudaSuccess)
+        return fail(PGEOF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(st.status));
+    const cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* err = error_bits;
+    if (!err) {
+        // the shared word keeps the previous call's bits: clear it first
+        PGEOF_CUDA_TRY(cudaMemsetAsync(st.err, 0, sizeof(uint32_t), s));
+        err = st.err;
+    }
+    if (n_points == 0) return PGEOF_OK;
+    if (n_xyz > 0) {
+        const unsigned blocks = (unsigned)std::min<uint64_t>(ceil_div_u((uint64_t)n_xyz, 256), 4096);
+        pad_xyz_kernel<<<blocks, 256, 0, s>>>(xyz, (uint64_t)n_xyz, st.xyz4);
+        count_launch();
+        PGEOF_TRY(check_launch("pad_xyz_kernel (noalloc)"));
+    }
+    FeatArgs a{};
+    a.xyz4 = st.xyz4;
+    a.n_xyz = (uint32_t)n_xyz;
+    a.nn = nn;
+    a.nnz = (uint64_t)nnz;
+    a.ptr = nn_ptr;
+    a.n_points = (uint32_t)n_points;
+    a.k_min = (uint32_t)std::min<uint64_t>(k_min, 0xffffffffull);
+    a.full = 1;
+    a.n_scales = 1;
+    a.scale_offset = 0;
+    a.out_scales = 1;
+    a.order = eig_order();
+    a.out = features;
+    a.err = err;
+    a.resolved = nullptr;
+    const size_t smem = (size_t)kFeatThreads * 11 * sizeof(float);
+    features_kernel<1><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
+    count_launch();
+    return check_launch("features_kernel (noalloc)");
+}
