@@ -2,28 +2,29 @@
 // (include/nn_search.hpp:31-132) and the radius-search + PCA path of
 // compute_features_selected (include/pgeof.hpp:325-375).
 //
-// One warp owns one query; queries are visited in cell order so neighbouring
-// warps read the same cells. Candidates are streamed as contiguous runs of the
-// cell-ordered point array: every row of cells (fixed y, z; a range of x) is one
-// run, runs are packed across the 32 lanes so no lane idles at row ends.
+// Candidates of a query are streamed as contiguous runs of the cell-ordered
+// point array: every row of cells (fixed y, z; a range of x) is one run, and
+// runs are packed across the 32 lanes so no lane idles at row ends. Distances
+// use nanoflann's metric_L2_Simple arithmetic -- (q - p)^2 per axis, summed x,
+// y, z, each operation rounded (no FMA) -- so values are bit-identical to the
+// reference's. Results are the exact smallest (d^2, index) pairs: ties at equal
+// distance order by index (nanoflann keeps its tree-traversal order there).
 //
-// Selection never keeps a sorted top-k list while scanning. Instead:
-//   A. grow a block of cells around the query until it holds >= k points
-//      (cell counts only, no point reads);
-//   B. one pass over that block builds a 32-bin histogram of squared distances,
-//      whose k-th-count bin edge tau^2 bounds the k-th neighbour distance;
-//   C. one pass over every cell within tau (rows clipped to the sphere) appends
-//      the points with d^2 <= tau^2 to a per-warp buffer -- usually ~1.2 k of
-//      them -- which is then bitonic-sorted by (d^2, index).
-// If pass C finds more points than the buffer holds, it refines instead: each
-// further pass histograms only the points inside the bin that contains the
-// k-th, first on d^2, then on the index when distances tie exactly, until the
-// survivors fit. The result is the exact k smallest (d^2, index) pairs.
-//
-// Distances use nanoflann's metric_L2_Simple arithmetic: (q - p)^2 per axis,
-// summed x, y, z, each operation rounded (no FMA), so values are bit-identical
-// to the reference's. Ties at equal distance order by index (nanoflann keeps
-// its tree-traversal order there).
+// Two kernels:
+//  * fast_search_kernel (float, k <= 128): a warp takes chunks of 32
+//    consecutive queries in cell order. One pass over the cells within a bound
+//    tau of the query appends every point with d^2 <= tau^2 to a shared-memory
+//    buffer; selection then runs in shared memory (64-bin distance histogram,
+//    counting-sort scatter of the bins up to the k-th, insertion sort inside the
+//    few-entry bins). For kNN, tau comes from the previous query of the chunk by
+//    the triangle inequality, d_k(q) <= d_k(prev) + |q - prev|, so most queries
+//    need no pilot pass; radius search uses tau = r. A query whose buffer
+//    overflows goes to a list for the general kernel.
+//  * search_kernel (float and double, any k): the general path. A pilot pass
+//    histograms a block of cells holding >= k points to bound the k-th distance,
+//    then passes over the cells within that bound refine a window of bins (first
+//    on d^2, then on the index when distances tie exactly) until the survivors
+//    fit the buffer.
 #include <algorithm>
 
 #include "eig3.cuh"
@@ -86,12 +87,19 @@ struct WarpSmem {
 };
 
 template <typename T>
-struct SearchArgs {
+struct GridView {
     GridParams g;
     const uint32_t* cell_start;
     const SPoint<T>* pts;
+};
+
+template <typename T>
+struct SearchArgs {
+    GridView<T> gv;
     const SPoint<T>* queries;
     uint64_t m;
+    const uint32_t* qlist;   // optional: positions in `queries` to process
+    const uint32_t* qcount;  // with qlist: number of entries (device)
     int mode;
     uint32_t k;
     T r2;
@@ -134,11 +142,12 @@ __device__ __forceinline__ float axis_gap(float v, int c, float o, float h, floa
     return fmaxf(0.0f, gap - margin);
 }
 
-// Visit every point of the cells in `bx` (rows clipped to the sphere of squared
-// radius R2 around q when prune). All lanes call visit(valid, d2, idx) together.
+// Visit every point of the cells in `bx` (rows clipped to the sphere of radius
+// Rf around q when prune). All lanes call visit(valid, d2, idx) together.
 template <typename T, typename F>
-__device__ __forceinline__ void visit_box(const SearchArgs<T>& a, WarpSmem<T>* ws, const T (&q)[3], const Box& bx,
-                                          bool prune, float Rf, F&& visit) {
+__device__ __forceinline__ void visit_box(const GridView<T>& gv, uint32_t* run_start, uint32_t* run_len,
+                                          const T (&q)[3], const Box& bx, bool prune, float Rf, F&& visit) {
+    const GridParams& g = gv.g;
     const int lane = threadIdx.x & 31;
     const int ny = bx.hi[1] - bx.lo[1] + 1, nz = bx.hi[2] - bx.lo[2] + 1;
     if (ny <= 0 || nz <= 0 || bx.hi[0] < bx.lo[0]) return;
@@ -153,21 +162,21 @@ __device__ __forceinline__ void visit_box(const SearchArgs<T>& a, WarpSmem<T>* w
             int xa = bx.lo[0], xb = bx.hi[0];
             bool keep = true;
             if (prune) {
-                const float gy = axis_gap(qf1, cy, a.g.oy, a.g.h, a.g.margin);
-                const float gz = axis_gap(qf2, cz, a.g.oz, a.g.h, a.g.margin);
+                const float gy = axis_gap(qf1, cy, g.oy, g.h, g.margin);
+                const float gz = axis_gap(qf2, cz, g.oz, g.h, g.margin);
                 const float dyz2 = gy * gy + gz * gz;
                 if (dyz2 > Rf2) {
                     keep = false;
                 } else {
-                    const float bxr = sqrtf(Rf2 - dyz2) + a.g.margin;
-                    xa = max(xa, cell_floor((qf0 - bxr - a.g.ox) * a.g.inv_h, a.g.gx));
-                    xb = min(xb, cell_floor((qf0 + bxr - a.g.ox) * a.g.inv_h, a.g.gx));
+                    const float bxr = sqrtf(Rf2 - dyz2) + g.margin;
+                    xa = max(xa, cell_floor((qf0 - bxr - g.ox) * g.inv_h, g.gx));
+                    xb = min(xb, cell_floor((qf0 + bxr - g.ox) * g.inv_h, g.gx));
                 }
             }
             if (keep && xa <= xb) {
-                const uint32_t base = ((uint32_t)cz * (uint32_t)a.g.gy + (uint32_t)cy) * (uint32_t)a.g.gx;
-                st = __ldg(a.cell_start + base + xa);
-                len = __ldg(a.cell_start + base + xb + 1) - st;
+                const uint32_t base = ((uint32_t)cz * (uint32_t)g.gy + (uint32_t)cy) * (uint32_t)g.gx;
+                st = __ldg(gv.cell_start + base + xa);
+                len = __ldg(gv.cell_start + base + xb + 1) - st;
             }
         }
         // pack the non-empty runs into lanes 0..nrows-1
@@ -176,12 +185,12 @@ __device__ __forceinline__ void visit_box(const SearchArgs<T>& a, WarpSmem<T>* w
         if (nrows == 0) continue;
         if (len > 0) {
             const int ci = __popc(ne & ((1u << lane) - 1u));
-            ws->run_start[ci] = st;
-            ws->run_len[ci] = len;
+            run_start[ci] = st;
+            run_len[ci] = len;
         }
         __syncwarp();
-        const uint32_t c_st = lane < nrows ? ws->run_start[lane] : 0u;
-        const uint32_t c_len = lane < nrows ? ws->run_len[lane] : 0u;
+        const uint32_t c_st = lane < nrows ? run_start[lane] : 0u;
+        const uint32_t c_len = lane < nrows ? run_len[lane] : 0u;
         __syncwarp();
         uint32_t incl = c_len;
 #pragma unroll
@@ -203,7 +212,7 @@ __device__ __forceinline__ void visit_box(const SearchArgs<T>& a, WarpSmem<T>* w
             T d2 = T(0);
             uint32_t idx = 0;
             if (valid) {
-                const SPoint<T> p = a.pts[r_st + (pos - r_ex)];
+                const SPoint<T> p = gv.pts[r_st + (pos - r_ex)];
                 d2 = dist2<T>(q, p);
                 idx = p.idx;
             }
@@ -211,6 +220,104 @@ __device__ __forceinline__ void visit_box(const SearchArgs<T>& a, WarpSmem<T>* w
             r_base = __popc(__ballot_sync(FULL, lane < nrows && excl <= base + 32)) - 1;
         }
     }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
+    return v;
+}
+
+__device__ __forceinline__ void query_cell(const GridParams& g, float x, float y, float z, int (&cq)[3]) {
+    const float v[3] = {x, y, z};
+    const float o[3] = {g.ox, g.oy, g.oz};
+    const int gd[3] = {g.gx, g.gy, g.gz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float c = (v[d] - o[d]) * g.inv_h;
+        cq[d] = (int)floorf(fminf(fmaxf(c, 0.0f), (float)(gd[d] - 1)));
+    }
+}
+
+// Pilot bound on the k-th neighbour distance: grow a block of cells around
+// the query until it holds >= k points (cell counts only), then a 32-bin
+// histogram of the block's squared distances gives tau^2 >= d_k^2.
+template <typename T>
+__device__ __forceinline__ T pilot_tau2(const GridView<T>& gv, uint32_t* hist32, uint32_t* run_start,
+                                        uint32_t* run_len, const T (&q)[3], uint32_t k) {
+    const GridParams& g = gv.g;
+    const int lane = threadIdx.x & 31;
+    const int gd[3] = {g.gx, g.gy, g.gz};
+    const float go[3] = {g.ox, g.oy, g.oz};
+    int cq[3];
+    query_cell(g, (float)q[0], (float)q[1], (float)q[2], cq);
+    Box bx;
+    for (int r = 0;; ++r) {
+        bool full = true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            bx.lo[d] = max(0, cq[d] - r);
+            bx.hi[d] = min(gd[d] - 1, cq[d] + r);
+            full = full && bx.lo[d] == 0 && bx.hi[d] == gd[d] - 1;
+        }
+        const int ny = bx.hi[1] - bx.lo[1] + 1, nz = bx.hi[2] - bx.lo[2] + 1;
+        uint32_t cnt = 0;
+        for (int row = lane; row < ny * nz; row += 32) {
+            const int cy = bx.lo[1] + row % ny, cz = bx.lo[2] + row / ny;
+            const uint32_t base = ((uint32_t)cz * (uint32_t)g.gy + (uint32_t)cy) * (uint32_t)g.gx;
+            cnt += __ldg(gv.cell_start + base + bx.hi[0] + 1) - __ldg(gv.cell_start + base + bx.lo[0]);
+        }
+        cnt = __reduce_add_sync(FULL, cnt);
+        if (cnt >= k || full) break;
+    }
+    float F2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float lo = go[d] + (float)bx.lo[d] * g.h, hi = go[d] + (float)(bx.hi[d] + 1) * g.h;
+        const float far = fmaxf((float)q[d] - lo, hi - (float)q[d]) + g.margin;
+        F2 += far * far;
+    }
+    const float sb = 32.0f / fmaxf(F2, 1e-30f);
+    hist32[lane] = 0;
+    __syncwarp();
+    T dmax = T(0);
+    visit_box<T>(gv, run_start, run_len, q, bx, false, 0.0f, [&](bool valid, T d2, uint32_t) {
+        if (valid) {
+            const float x = (float)d2 * sb;
+            const int bin = x >= 31.0f ? 31 : (int)x;
+            atomicAdd(&hist32[bin], 1u);
+            dmax = max(dmax, d2);
+        }
+    });
+    __syncwarp();
+    dmax = warp_max(dmax);
+    uint32_t incl = hist32[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    __syncwarp();
+    const uint32_t reach = __ballot_sync(FULL, incl >= k);
+    const int b = reach ? __ffs(reach) - 1 : 31;
+    T tau2 = dmax;
+    if (b < 31) tau2 = min(dmax, (T)(((float)(b + 1) / sb) * 1.000004f));
+    return tau2;
+}
+
+// Cells within distance tf of q (a conservative box).
+__device__ __forceinline__ Box region_box(const GridParams& g, float qx, float qy, float qz, float tf) {
+    const float v[3] = {qx, qy, qz};
+    const float o[3] = {g.ox, g.oy, g.oz};
+    const int gd[3] = {g.gx, g.gy, g.gz};
+    Box rb;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        rb.lo[d] = max(0, cell_floor((v[d] - tf - o[d]) * g.inv_h, gd[d]));
+        rb.hi[d] = min(gd[d] - 1, cell_floor((v[d] + tf - o[d]) * g.inv_h, gd[d]));
+    }
+    return rb;
 }
 
 template <typename T>
@@ -260,13 +367,40 @@ __device__ __forceinline__ void bitonic_sort(Entry<T>* buf, int n, int P) {
     }
 }
 
-template <typename T>
-__device__ __forceinline__ T warp_max(T v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL, v, o));
-    return v;
+// Write one query's result row (knn: k entries; radius: -1 / 0 padding and
+// nanoflann's radius^2 in the last slot of a short row).
+template <typename T, typename GetEntry>
+__device__ __forceinline__ void emit_row(int mode, uint32_t k, uint32_t n_sel, uint32_t found, uint64_t qo,
+                                         void* out_idx, T* out_d2, uint32_t* out_found, int fill_last, T r2,
+                                         GetEntry&& get) {
+    const int lane = threadIdx.x & 31;
+    if (mode == MODE_KNN) {
+        uint32_t* oi = static_cast<uint32_t*>(out_idx) + qo * k;
+        T* od = out_d2 ? out_d2 + qo * k : nullptr;
+        for (uint32_t j = lane; j < k; j += 32) {
+            const Entry<T> e = get(j);
+            oi[j] = e.idx;
+            if (od) od[j] = e.d2;
+        }
+    } else {
+        const uint32_t nk = min(n_sel, k);
+        int32_t* oi = static_cast<int32_t*>(out_idx) + qo * k;
+        T* od = out_d2 ? out_d2 + qo * k : nullptr;
+        for (uint32_t j = lane; j < k; j += 32) {
+            if (j < nk) {
+                const Entry<T> e = get(j);
+                oi[j] = (int32_t)e.idx;
+                if (od) od[j] = e.d2;
+            } else {
+                oi[j] = -1;
+                if (od) od[j] = (fill_last && j == k - 1) ? r2 : T(0);
+            }
+        }
+        if (out_found && lane == 0) out_found[qo] = found;
+    }
 }
 
+// ------------------------------------------------------------------ general
 template <typename T>
 __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_constant__ SearchArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -276,89 +410,25 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
                         ? reinterpret_cast<Entry<T>*>(smem_raw + kSearchWarps * sizeof(WarpSmem<T>)) + (size_t)wib * a.cap
                         : a.gbuf + ((size_t)blockIdx.x * kSearchWarps + wib) * a.cap;
     const uint64_t nwarps = (uint64_t)gridDim.x * kSearchWarps;
-    const GridParams& g = a.g;
-    const int gd[3] = {g.gx, g.gy, g.gz};
-    const float go[3] = {g.ox, g.oy, g.oz};
+    const GridParams& g = a.gv.g;
+    const uint64_t m = a.qlist ? (uint64_t)*a.qcount : a.m;
 
-    for (uint64_t qi = (uint64_t)blockIdx.x * kSearchWarps + wib; qi < a.m; qi += nwarps) {
-        const SPoint<T> qp = a.queries[qi];
+    for (uint64_t qi = (uint64_t)blockIdx.x * kSearchWarps + wib; qi < m; qi += nwarps) {
+        const SPoint<T> qp = a.queries[a.qlist ? a.qlist[qi] : qi];
         const T q[3] = {qp.x, qp.y, qp.z};
         const uint32_t k = a.k;
-        int cq[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const float c = ((float)q[d] - go[d]) * g.inv_h;
-            cq[d] = (int)floorf(fminf(fmaxf(c, 0.0f), (float)(gd[d] - 1)));
-        }
         T tau2;
         bool strict;
         if (a.mode == MODE_KNN) {
-            // A. grow a cell block until it holds >= k points
-            Box bx;
-            for (int r = 0;; ++r) {
-                bool full = true;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    bx.lo[d] = max(0, cq[d] - r);
-                    bx.hi[d] = min(gd[d] - 1, cq[d] + r);
-                    full = full && bx.lo[d] == 0 && bx.hi[d] == gd[d] - 1;
-                }
-                const int ny = bx.hi[1] - bx.lo[1] + 1, nz = bx.hi[2] - bx.lo[2] + 1;
-                uint32_t cnt = 0;
-                for (int row = lane; row < ny * nz; row += 32) {
-                    const int cy = bx.lo[1] + row % ny, cz = bx.lo[2] + row / ny;
-                    const uint32_t base = ((uint32_t)cz * (uint32_t)g.gy + (uint32_t)cy) * (uint32_t)g.gx;
-                    cnt += __ldg(a.cell_start + base + bx.hi[0] + 1) - __ldg(a.cell_start + base + bx.lo[0]);
-                }
-                cnt = __reduce_add_sync(FULL, cnt);
-                if (cnt >= k || full) break;
-            }
-            // B. histogram of d^2 over the block -> tau^2 >= k-th distance^2
-            float F2 = 0.0f;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const float lo = go[d] + (float)bx.lo[d] * g.h, hi = go[d] + (float)(bx.hi[d] + 1) * g.h;
-                const float far = fmaxf((float)q[d] - lo, hi - (float)q[d]) + g.margin;
-                F2 += far * far;
-            }
-            const float sb = 32.0f / fmaxf(F2, 1e-30f);
-            ws->hist[lane] = 0;
-            __syncwarp();
-            T dmax = T(0);
-            visit_box<T>(a, ws, q, bx, false, 0.0f, [&](bool valid, T d2, uint32_t) {
-                if (valid) {
-                    const float x = (float)d2 * sb;
-                    const int bin = x >= 31.0f ? 31 : (int)x;
-                    atomicAdd(&ws->hist[bin], 1u);
-                    dmax = max(dmax, d2);
-                }
-            });
-            __syncwarp();
-            dmax = warp_max(dmax);
-            uint32_t hv = ws->hist[lane], incl = hv;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL, incl, o);
-                if (lane >= o) incl += y;
-            }
-            const uint32_t reach = __ballot_sync(FULL, incl >= k);
-            const int b = reach ? __ffs(reach) - 1 : 31;
-            tau2 = dmax;
-            if (b < 31) tau2 = min(dmax, (T)(((float)(b + 1) / sb) * 1.000004f));
+            tau2 = pilot_tau2<T>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
             strict = false;
         } else {
             tau2 = a.r2;
             strict = true;
         }
-
-        // C. collect every point within tau (refining when the buffer overflows)
+        // collect every point within tau (refining when the buffer overflows)
         const float tf = sqrtf((float)tau2) * 1.000001f + g.margin;
-        Box rb;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            rb.lo[d] = max(0, cell_floor(((float)q[d] - tf - go[d]) * g.inv_h, gd[d]));
-            rb.hi[d] = min(gd[d] - 1, cell_floor(((float)q[d] + tf - go[d]) * g.inv_h, gd[d]));
-        }
+        const Box rb = region_box(g, (float)q[0], (float)q[1], (float)q[2], tf);
         Level<T> H;  // histogram spec for the current window
         H.type = 0;
         H.lo = T(0);
@@ -376,7 +446,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
             ws->imax[lane] = 0;
             __syncwarp();
             uint32_t count = 0;
-            visit_box<T>(a, ws, q, rb, true, tf, [&](bool valid, T d2, uint32_t idx) {
+            visit_box<T>(a.gv, ws->run_start, ws->run_len, q, rb, true, tf, [&](bool valid, T d2, uint32_t idx) {
                 const bool member = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
                 const int st = member ? classify<T>(ws, nlev, d2, idx) : 2;
                 const bool take = st != 2;
@@ -450,32 +520,233 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
         int P = 1;
         while (P < (int)n_sel) P <<= 1;
         if (n_sel > 1) bitonic_sort<T>(buf, (int)n_sel, P);
-        const uint64_t qo = qp.idx;
-        if (a.mode == MODE_KNN) {
-            uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + qo * k;
-            T* od = a.out_d2 ? a.out_d2 + qo * k : nullptr;
-            for (uint32_t j = lane; j < k; j += 32) {
-                const Entry<T> e = buf[j];
-                oi[j] = e.idx;
-                if (od) od[j] = e.d2;
-            }
-        } else {
-            const uint32_t nk = min(n_sel, k);
-            int32_t* oi = static_cast<int32_t*>(a.out_idx) + qo * k;
-            T* od = a.out_d2 ? a.out_d2 + qo * k : nullptr;
-            for (uint32_t j = lane; j < k; j += 32) {
-                if (j < nk) {
-                    const Entry<T> e = buf[j];
-                    oi[j] = (int32_t)e.idx;
-                    if (od) od[j] = e.d2;
-                } else {
-                    oi[j] = -1;
-                    if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : T(0);
+        emit_row<T>(a.mode, k, n_sel, found, qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
+                    [&](uint32_t j) { return buf[j]; });
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------------ fast (float)
+constexpr int kFastWarps = 4;
+constexpr int kChunk = 32;       // consecutive queries per work item
+constexpr int kSelBins = 64;     // selection histogram
+constexpr int kMaxInBin = 24;    // larger bins (exact ties) fall back to a bitonic sort
+
+struct FastArgs {
+    GridView<float> gv;
+    const SPoint<float>* queries;
+    uint64_t m;
+    int mode;
+    uint32_t k;
+    float r2;
+    uint32_t cap;  // power of two, buffer entries per warp
+    uint32_t* work;
+    uint32_t* ovf_list;
+    uint32_t* ovf_count;
+    void* out_idx;
+    float* out_d2;
+    uint32_t* out_found;
+    int fill_last;
+    uint32_t* err;
+};
+
+struct FastWarpSmem {
+    uint32_t hist[kSelBins];
+    uint32_t cursor[kSelBins];
+    uint32_t run_start[32], run_len[32];
+};
+
+__device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
+    return ((uint64_t)__float_as_uint(d2) << 32) | idx;
+}
+__device__ __forceinline__ float key_d2(uint64_t key) { return __uint_as_float((uint32_t)(key >> 32)); }
+
+// bitonic sort of keys[0..n) padded to P with ~0 (larger than any key)
+__device__ __forceinline__ void bitonic_keys(uint64_t* keys, int n, int P) {
+    const int lane = threadIdx.x & 31;
+    for (int i = n + lane; i < P; i += 32) keys[i] = ~0ull;
+    __syncwarp();
+    for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < P / 2; t += 32) {
+                const int i = 2 * stride * (t / stride) + (t % stride);
+                const int j = i + stride;
+                const bool up = (i & size) == 0;
+                const uint64_t x = keys[i], y = keys[j];
+                if ((y < x) == up) {
+                    keys[i] = y;
+                    keys[j] = x;
                 }
             }
-            if (a.out_found && lane == 0) a.out_found[qo] = found;
+            __syncwarp();
         }
+    }
+}
+
+// Sort the n_sel smallest of keys[0..count) into out[0..n_sel) (count <= cap,
+// every key has d^2 <= tau2). Returns nothing; out is fully ordered up to the
+// last bin that contains the n_sel-th key.
+__device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* keys, uint32_t count,
+                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t cap) {
+    const int lane = threadIdx.x & 31;
+    const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
+    ws->hist[lane] = 0;
+    ws->hist[lane + 32] = 0;
+    __syncwarp();
+    for (uint32_t i = lane; i < count; i += 32) {
+        const float x = key_d2(keys[i]) * sb;
+        const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
+        atomicAdd(&ws->hist[bin], 1u);
+    }
+    __syncwarp();
+    // lane owns bins 2*lane, 2*lane+1
+    const uint32_t h0 = ws->hist[2 * lane], h1 = ws->hist[2 * lane + 1];
+    uint32_t incl = h0 + h1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t excl = incl - h0 - h1;
+    ws->cursor[2 * lane] = excl;
+    ws->cursor[2 * lane + 1] = excl + h0;
+    // last bin needed: first bin whose inclusive count reaches n_sel
+    const bool reach0 = excl + h0 >= n_sel, reach1 = incl >= n_sel;
+    const uint32_t r0 = __ballot_sync(FULL, reach0), r1 = __ballot_sync(FULL, reach1);
+    int bstar = kSelBins - 1;
+    if (r0 | r1) {
+        const int l0 = r0 ? __ffs(r0) - 1 : 64, l1 = r1 ? __ffs(r1) - 1 : 64;
+        bstar = min(2 * l0, 2 * l1 + 1);
+    }
+    const uint32_t big = __ballot_sync(FULL, (2 * lane <= bstar && h0 > kMaxInBin) ||
+                                                 (2 * lane + 1 <= bstar && h1 > kMaxInBin));
+    __syncwarp();
+    uint32_t n_take = 0;
+    {
+        const int lb = bstar >> 1;
+        const uint32_t e = __shfl_sync(FULL, excl, lb), hh0 = __shfl_sync(FULL, h0, lb),
+                       hh1 = __shfl_sync(FULL, h1, lb);
+        n_take = (bstar & 1) ? e + hh0 + hh1 : e + hh0;
+    }
+    for (uint32_t i = lane; i < count; i += 32) {
+        const uint64_t key = keys[i];
+        const float x = key_d2(key) * sb;
+        const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
+        if (bin <= bstar) out[atomicAdd(&ws->cursor[bin], 1u)] = key;
+    }
+    __syncwarp();
+    if (big) {
+        // exact ties crowd a bin: sort the whole prefix
+        int P = 1;
+        while (P < (int)n_take) P <<= 1;
+        if (P <= (int)cap) bitonic_keys(out, (int)n_take, P);
         __syncwarp();
+        return;
+    }
+    // insertion sort inside each bin (a handful of keys each)
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int bin = 2 * lane + t;
+        if (bin <= bstar) {
+            const uint32_t end = ws->cursor[bin];
+            const uint32_t beg = end - (t ? h1 : h0);
+            for (uint32_t i = beg + 1; i < end; ++i) {
+                const uint64_t v = out[i];
+                uint32_t j = i;
+                while (j > beg && out[j - 1] > v) {
+                    out[j] = out[j - 1];
+                    --j;
+                }
+                out[j] = v;
+            }
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __grid_constant__ FastArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    FastWarpSmem* ws = reinterpret_cast<FastWarpSmem*>(smem_raw) + wib;
+    uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw + kFastWarps * sizeof(FastWarpSmem)) +
+                     (size_t)wib * 2 * a.cap;
+    uint64_t* sorted = keys + a.cap;
+    const GridParams& g = a.gv.g;
+    const uint32_t k = a.k;
+    for (;;) {
+        uint32_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.work, 1u);
+        chunk = __shfl_sync(FULL, chunk, 0);
+        const uint64_t q0 = (uint64_t)chunk * kChunk;
+        if (q0 >= a.m) break;
+        const uint64_t q1 = min(q0 + (uint64_t)kChunk, a.m);
+        bool have_prev = false;
+        float prev_dk = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+        for (uint64_t qi = q0; qi < q1; ++qi) {
+            const SPoint<float> qp = a.queries[qi];
+            const float q[3] = {qp.x, qp.y, qp.z};
+            float tau2;
+            bool strict;
+            if (a.mode == MODE_KNN) {
+                strict = false;
+                bool tri = false;
+                if (have_prev) {
+                    const float dx = q[0] - px, dy = q[1] - py, dz = q[2] - pz;
+                    const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
+                    if (dq <= 0.5f * prev_dk) {
+                        // d_k(q) <= d_k(prev) + |q - prev|, inflated for rounding
+                        const float t = (prev_dk + dq) * 1.00002f + 1e-30f + g.margin * 1e-3f;
+                        tau2 = t * t;
+                        tri = true;
+                    }
+                }
+                if (!tri) tau2 = pilot_tau2<float>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
+            } else {
+                strict = true;
+                tau2 = a.r2;
+            }
+            const float tf = sqrtf(tau2) * 1.000001f + g.margin;
+            const Box rb = region_box(g, q[0], q[1], q[2], tf);
+            uint32_t count = 0;
+            visit_box<float>(a.gv, ws->run_start, ws->run_len, q, rb, true, tf,
+                             [&](bool valid, float d2, uint32_t idx) {
+                                 const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
+                                 const uint32_t mask = __ballot_sync(FULL, take);
+                                 if (take) {
+                                     const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
+                                     if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                                 }
+                                 count += __popc(mask);
+                             });
+            __syncwarp();
+            const bool short_knn = a.mode == MODE_KNN && count < k;  // rounding corner: never expected
+            if (count > a.cap || short_knn) {
+                if (lane == 0) {
+                    const uint32_t slot = atomicAdd(a.ovf_count, 1u);
+                    a.ovf_list[slot] = (uint32_t)qi;
+                }
+                have_prev = false;
+                continue;
+            }
+            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
+            if (n_sel > 0) select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap);
+            emit_row<float>(a.mode, k, n_sel, count, qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
+                            [&](uint32_t j) {
+                                const uint64_t key = sorted[j];
+                                Entry<float> e;
+                                e.d2 = key_d2(key);
+                                e.idx = (uint32_t)key;
+                                return e;
+                            });
+            if (a.mode == MODE_KNN) {
+                prev_dk = sqrtf(key_d2(sorted[k - 1]));
+                px = q[0];
+                py = q[1];
+                pz = q[2];
+                have_prev = true;
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -561,25 +832,22 @@ __global__ void __launch_bounds__(kSelThreads) selected_pca_kernel(const __grid_
 }
 
 template <typename T>
-int smem_bytes(uint32_t cap, bool in_smem) {
+int general_smem_bytes(uint32_t cap, bool in_smem) {
     return (int)(kSearchWarps * (sizeof(WarpSmem<T>) + (in_smem ? (size_t)cap * sizeof(Entry<T>) : 0)));
 }
 
-}  // namespace
-
 template <typename T>
-int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, int mode, uint32_t k, T radius,
-                  const SearchOut<T>& out, cudaStream_t s) {
-    if (m == 0 || k == 0) return PGEOF_OK;
-    if (grid.n == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "search over an empty point cloud");
+int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, const uint32_t* qlist,
+                   const uint32_t* qcount, int mode, uint32_t k, T radius, const SearchOut<T>& out,
+                   cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     // buffer capacity: a power of two comfortably above k
-    uint64_t want = mode == MODE_KNN ? std::max<uint64_t>(2ull * k, 128) : std::max<uint64_t>(4ull * k, 256);
+    const uint64_t want = mode == MODE_KNN ? std::max<uint64_t>(2ull * k, 128) : std::max<uint64_t>(4ull * k, 256);
     uint32_t cap = 1;
     while (cap < want) cap <<= 1;
-    bool in_smem = smem_bytes<T>(cap, true) <= std::min(di->max_smem_optin, 200 * 1024);
-    const int smem = smem_bytes<T>(cap, in_smem);
+    const bool in_smem = general_smem_bytes<T>(cap, true) <= std::min(di->max_smem_optin, 200 * 1024);
+    const int smem = general_smem_bytes<T>(cap, in_smem);
     auto kern = search_kernel<T>;
     if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
@@ -592,11 +860,13 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m
         PGEOF_TRY(gbuf.alloc(blocks * kSearchWarps * (size_t)cap * sizeof(Entry<T>), s));
         a.gbuf = gbuf.as<Entry<T>>();
     }
-    a.g = grid.g;
-    a.cell_start = grid.cell_start;
-    a.pts = grid.pts;
+    a.gv.g = grid.g;
+    a.gv.cell_start = grid.cell_start;
+    a.gv.pts = grid.pts;
     a.queries = queries;
     a.m = m;
+    a.qlist = qlist;
+    a.qcount = qcount;
     a.mode = mode;
     a.k = k;
     a.r2 = (T)(radius * radius);  // sq_search_radius in real_t, nn_search.hpp:98
@@ -607,10 +877,70 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m
     a.out_found = out.found;
     a.fill_last = out.radius_fill_last ? 1 : 0;
     a.err = device_error_word();
-    KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
+    KernelTimer kt(qlist ? "overflow_search_kernel" : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel"),
+                   s);
     kern<<<(unsigned)blocks, kSearchWarps * 32, smem, s>>>(a);
     count_launch();
     return check_launch("search_kernel");
+}
+
+}  // namespace
+
+template <typename T>
+int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, int mode, uint32_t k, T radius,
+                  const SearchOut<T>& out, cudaStream_t s) {
+    if (m == 0 || k == 0) return PGEOF_OK;
+    if (grid.n == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "search over an empty point cloud");
+    if constexpr (sizeof(T) != sizeof(float)) {
+        return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
+    } else {
+    if (k > 128 || m >= 0xffffffffull)
+        return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
+    const DeviceInfo* di;
+    PGEOF_TRY(current_device_info(&di));
+    uint32_t cap = 1;
+    const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? 256 : 512, 4ull * k);
+    while (cap < want) cap <<= 1;
+    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + 2 * (size_t)cap * sizeof(uint64_t)));
+    if (smem > 48 * 1024)
+        PGEOF_CUDA_TRY(cudaFuncSetAttribute(fast_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int per_sm = 0;
+    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fast_search_kernel, kFastWarps * 32, smem));
+    per_sm = std::max(per_sm, 1);
+    const uint64_t chunks = ceil_div_u(m, kChunk);
+    const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
+    // work counter, overflow count, overflow list
+    Scratch ctl;
+    PGEOF_TRY(ctl.alloc((m + 8) * sizeof(uint32_t), s));
+    uint32_t* words = ctl.as<uint32_t>();
+    PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
+    FastArgs a{};
+    a.gv.g = grid.g;
+    a.gv.cell_start = grid.cell_start;
+    a.gv.pts = reinterpret_cast<const SPoint<float>*>(grid.pts);
+    a.queries = reinterpret_cast<const SPoint<float>*>(queries);
+    a.m = m;
+    a.mode = mode;
+    a.k = k;
+    a.r2 = (float)(radius * radius);  // sq_search_radius in real_t, nn_search.hpp:98
+    a.cap = cap;
+    a.work = words;
+    a.ovf_count = words + 1;
+    a.ovf_list = words + 8;
+    a.out_idx = out.indices;
+    a.out_d2 = reinterpret_cast<float*>(out.sqr_dist);
+    a.out_found = out.found;
+    a.fill_last = out.radius_fill_last ? 1 : 0;
+    a.err = device_error_word();
+    {
+        KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
+        fast_search_kernel<<<(unsigned)blocks, kFastWarps * 32, smem, s>>>(a);
+    }
+    count_launch();
+    PGEOF_TRY(check_launch("fast_search_kernel"));
+    // queries whose buffer overflowed: the general kernel, sized on the device
+    return launch_general<T>(grid, queries, m, a.ovf_list, a.ovf_count, mode, k, radius, out, s);
+    }
 }
 
 template <typename T>
