@@ -167,13 +167,17 @@ int knn_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_
     if (n_query == 0 || knn == 0) return PGEOF_OK;
     GridIndex<float> grid;
     PGEOF_TRY(build_grid<float>(data, n_data, knn, 0.0f, 0.0f, grid, s));
-    const SPoint<float>* q = grid.pts;
-    Scratch qmem;
-    if (!query_is_data) PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, const_cast<SPoint<float>**>(&q), s));
+    SPoint<float>* q = grid.pts;
+    const uint32_t* qstart = grid.cell_start;
+    Scratch qmem, qstart_mem;
+    if (!query_is_data) {
+        PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, &q, qstart_mem, s));
+        qstart = qstart_mem.as<uint32_t>();
+    }
     SearchOut<float> out;
     out.indices = indices;
     out.sqr_dist = sqr_dist;
-    return launch_search<float>(grid, q, n_query, MODE_KNN, knn, 0.0f, out, s);
+    return launch_search<float>(grid, q, qstart, n_query, MODE_KNN, knn, 0.0f, out, s);
 }
 
 int radius_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_query, float radius,
@@ -182,14 +186,18 @@ int radius_impl(const float* data, uint64_t n_data, const float* query, uint64_t
     GridIndex<float> grid;
     const float r = std::fabs(radius);
     PGEOF_TRY(build_grid<float>(data, n_data, max_knn, r / 4.0f, r, grid, s));
-    const SPoint<float>* q = grid.pts;
-    Scratch qmem;
-    if (!query_is_data) PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, const_cast<SPoint<float>**>(&q), s));
+    SPoint<float>* q = grid.pts;
+    const uint32_t* qstart = grid.cell_start;
+    Scratch qmem, qstart_mem;
+    if (!query_is_data) {
+        PGEOF_TRY(sort_queries<float>(query, n_query, grid.g, qmem, &q, qstart_mem, s));
+        qstart = qstart_mem.as<uint32_t>();
+    }
     SearchOut<float> out;
     out.indices = indices;
     out.sqr_dist = sqr_dist;
     out.radius_fill_last = true;
-    return launch_search<float>(grid, q, n_query, MODE_RADIUS, max_knn, radius, out, s);
+    return launch_search<float>(grid, q, qstart, n_query, MODE_RADIUS, max_knn, radius, out, s);
 }
 
 int features_impl(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* nn_ptr,
@@ -223,7 +231,7 @@ int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const in
     so.sqr_dist = nullptr;
     so.found = found.as<uint32_t>();
     so.radius_fill_last = false;
-    PGEOF_TRY(launch_search<T>(grid, grid.pts, n, MODE_RADIUS, k_search, radius, so, s));
+    PGEOF_TRY(launch_search<T>(grid, grid.pts, grid.cell_start, n, MODE_RADIUS, k_search, radius, so, s));
     return launch_selected_pca<T>(xyz, n, nbr.as<int32_t>(), found.as<uint32_t>(), max_knn, ids, (int)n_ids, out,
                                   s);
 }

@@ -10,7 +10,7 @@
 #include <cstdio>
 #include <string>
 
-#include "../../include/pgeof_cuda.h"
+#include "pgeof_cuda.h"
 
 namespace pgeof {
 

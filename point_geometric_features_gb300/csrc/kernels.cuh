@@ -57,9 +57,11 @@ template <typename T>
 int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h_max, GridIndex<T>& out,
                cudaStream_t s);
 
-// Counting-sort arbitrary query points into `grid`'s cell order.
+// Counting-sort arbitrary query points into `grid`'s cell order; `start`
+// receives the per-cell offsets of the sorted queries (n_cells + 1).
 template <typename T>
-int sort_queries(const T* q, uint64_t m, const GridParams& g, Scratch& out_mem, SPoint<T>** out, cudaStream_t s);
+int sort_queries(const T* q, uint64_t m, const GridParams& g, Scratch& out_mem, SPoint<T>** out, Scratch& start,
+                 cudaStream_t s);
 
 // ----------------------------------------------------------- neighbour search
 enum SearchMode { MODE_KNN = 0, MODE_RADIUS = 1 };
@@ -72,9 +74,11 @@ struct SearchOut {
     bool radius_fill_last = true;     // nanoflann RKNN: radius^2 in the last slot of short rows
 };
 
+// `queries` are in `grid`'s cell order; `qstart` (n_cells + 1) gives each
+// cell's range of them (grid.cell_start when the queries are the points).
 template <typename T>
-int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, int mode, uint32_t k, T radius,
-                  const SearchOut<T>& out, cudaStream_t s);
+int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint32_t* qstart, uint64_t m, int mode,
+                  uint32_t k, T radius, const SearchOut<T>& out, cudaStream_t s);
 
 // PCA + selected features from a radius-search neighbour table (selected path).
 template <typename T>

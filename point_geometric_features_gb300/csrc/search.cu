@@ -16,9 +16,10 @@
 //    tau of the query appends every point with d^2 <= tau^2 to a shared-memory
 //    buffer; selection then runs in shared memory (64-bin distance histogram,
 //    counting-sort scatter of the bins up to the k-th, insertion sort inside the
-//    few-entry bins). For kNN, tau comes from the previous query of the chunk by
-//    the triangle inequality, d_k(q) <= d_k(prev) + |q - prev|, so most queries
-//    need no pilot pass; radius search uses tau = r. A query whose buffer
+//    few-entry bins). For kNN, tau comes from the queries the warp solved last
+//    (one per lane) by the triangle inequality, d_k(q) <= d_k(p) + |q - p|,
+//    minimised over the lanes, so only the first query of a chunk needs a pilot
+//    pass; radius search uses tau = r. A query whose buffer
 //    overflows goes to a list for the general kernel.
 //  * search_kernel (float and double, any k): the general path. A pilot pass
 //    histograms a block of cells holding >= k points to bound the k-th distance,
@@ -528,7 +529,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
 
 // ------------------------------------------------------------------ fast (float)
 constexpr int kFastWarps = 4;
-constexpr int kChunk = 32;       // consecutive queries per work item
+constexpr int kChunk = 64;       // consecutive queries per work item
 constexpr int kSelBins = 64;     // selection histogram
 constexpr int kMaxInBin = 24;    // larger bins (exact ties) fall back to a bitonic sort
 
@@ -680,8 +681,8 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
         const uint64_t q0 = (uint64_t)chunk * kChunk;
         if (q0 >= a.m) break;
         const uint64_t q1 = min(q0 + (uint64_t)kChunk, a.m);
-        bool have_prev = false;
-        float prev_dk = 0.0f, px = 0.0f, py = 0.0f, pz = 0.0f;
+        // the last 32 solved queries of this chunk, one per lane: position and d_k
+        float rx = 0.0f, ry = 0.0f, rz = 0.0f, rdk = -1.0f;
         for (uint64_t qi = q0; qi < q1; ++qi) {
             const SPoint<float> qp = a.queries[qi];
             const float q[3] = {qp.x, qp.y, qp.z};
@@ -689,18 +690,20 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             bool strict;
             if (a.mode == MODE_KNN) {
                 strict = false;
-                bool tri = false;
-                if (have_prev) {
-                    const float dx = q[0] - px, dy = q[1] - py, dz = q[2] - pz;
+                // d_k(q) <= d_k(p) + |q - p| for every solved p: take the best over the lanes
+                float bound = INFINITY;
+                if (rdk >= 0.0f) {
+                    const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
                     const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (dq <= 0.5f * prev_dk) {
-                        // d_k(q) <= d_k(prev) + |q - prev|, inflated for rounding
-                        const float t = (prev_dk + dq) * 1.00002f + 1e-30f + g.margin * 1e-3f;
-                        tau2 = t * t;
-                        tri = true;
-                    }
+                    if (dq <= 0.75f * rdk) bound = rdk + dq;
                 }
-                if (!tri) tau2 = pilot_tau2<float>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
+                if (bound < INFINITY) {
+                    const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
+                    tau2 = t * t;
+                } else {
+                    tau2 = pilot_tau2<float>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                }
             } else {
                 strict = true;
                 tau2 = a.r2;
@@ -725,7 +728,6 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                     const uint32_t slot = atomicAdd(a.ovf_count, 1u);
                     a.ovf_list[slot] = (uint32_t)qi;
                 }
-                have_prev = false;
                 continue;
             }
             const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
@@ -738,12 +740,11 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                                 e.idx = (uint32_t)key;
                                 return e;
                             });
-            if (a.mode == MODE_KNN) {
-                prev_dk = sqrtf(key_d2(sorted[k - 1]));
-                px = q[0];
-                py = q[1];
-                pz = q[2];
-                have_prev = true;
+            if (a.mode == MODE_KNN && lane == (int)(qi & 31)) {
+                rdk = sqrtf(key_d2(sorted[k - 1]));
+                rx = q[0];
+                ry = q[1];
+                rz = q[2];
             }
             __syncwarp();
         }
@@ -887,8 +888,8 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
 }  // namespace
 
 template <typename T>
-int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, int mode, uint32_t k, T radius,
-                  const SearchOut<T>& out, cudaStream_t s) {
+int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint32_t* /*qstart*/, uint64_t m,
+                  int mode, uint32_t k, T radius, const SearchOut<T>& out, cudaStream_t s) {
     if (m == 0 || k == 0) return PGEOF_OK;
     if (grid.n == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "search over an empty point cloud");
     if constexpr (sizeof(T) != sizeof(float)) {
@@ -968,10 +969,10 @@ int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint
     return PGEOF_OK;
 }
 
-template int launch_search<float>(const GridIndex<float>&, const SPoint<float>*, uint64_t, int, uint32_t, float,
-                                  const SearchOut<float>&, cudaStream_t);
-template int launch_search<double>(const GridIndex<double>&, const SPoint<double>*, uint64_t, int, uint32_t, double,
-                                   const SearchOut<double>&, cudaStream_t);
+template int launch_search<float>(const GridIndex<float>&, const SPoint<float>*, const uint32_t*, uint64_t, int,
+                                  uint32_t, float, const SearchOut<float>&, cudaStream_t);
+template int launch_search<double>(const GridIndex<double>&, const SPoint<double>*, const uint32_t*, uint64_t, int,
+                                   uint32_t, double, const SearchOut<double>&, cudaStream_t);
 template int launch_selected_pca<float>(const float*, uint64_t, const int32_t*, const uint32_t*, uint32_t,
                                         const int32_t*, int, float*, cudaStream_t);
 template int launch_selected_pca<double>(const double*, uint64_t, const int32_t*, const uint32_t*, uint32_t,
