@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
+    p.add_argument("--workload", choices=["scene", "batch"], default="scene",
+                   help="scene: the headline 1M-point kNN+multiscale step; batch: 256 clouds, plain vs batched")
     return p.parse_args()
 
 
@@ -393,9 +395,79 @@ def run_reference(args, rank, world):
     }
 
 
+def run_batch(args):
+    """configs[3]: 256 clouds, sizes log-uniform in [2,000, 200,000] (seed 3),
+    each the outdoor-scene generator scaled to a cube side U(5, 50) m; knn k=32
+    plus compute_features. Plain: one knn_search + one compute_features call per
+    cloud. Batched: the whole batch as one CUDA-graph replay."""
+    import torch
+
+    import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.synthetic import log_uniform_sizes, scaled_scene
+
+    torch.cuda.set_device(0)
+    k = 32
+    sizes = log_uniform_sizes(256, 2_000, 200_000, seed=3)
+    rng = np.random.default_rng(3)
+    clouds = [torch.from_numpy(scaled_scene(int(n), seed=3000 + i, side=float(rng.uniform(5.0, 50.0)))).cuda()
+              for i, n in enumerate(sizes)]
+    n_total = int(sum(int(c.shape[0]) for c in clouds))
+    ptrs = [torch.arange(0, k * (c.shape[0] + 1), k, dtype=torch.int32, device="cuda") for c in clouds]
+
+    def plain():
+        for c, ptr in zip(clouds, ptrs):
+            idx, _ = pgeof.knn_search(c, c, k)
+            pgeof.compute_features(c, idx.view(-1), ptr, check=False)
+
+    plan = pgeof.BatchPlan(clouds, k)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for _ in range(max(args.warmup, 3)):
+        plain()
+        plan()
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(args.steps):
+        plain()
+    ev[1].record()
+    for _ in range(args.steps):
+        plan()
+    ev[2].record()
+    torch.cuda.synchronize()
+    plain_ms = ev[0].elapsed_time(ev[1]) / args.steps
+    batch_ms = ev[1].elapsed_time(ev[2]) / args.steps
+    # the graph replay must reproduce the per-cloud results
+    bi, bd, bf = plan()
+    torch.cuda.synchronize()
+    ok = True
+    off = 0
+    for c in clouds[:8]:
+        i, d = pgeof.knn_search(c, c, k)
+        ok &= bool(torch.equal(i.to(torch.int64), bi[off:off + c.shape[0]].to(torch.int64)))
+        off += c.shape[0]
+    plan.close()
+    return {
+        "metric": METRIC,
+        "workload": "batch",
+        "config": {"clouds": 256, "points": n_total, "sizes": "log-uniform [2000, 200000], seed 3",
+                   "k": k, "features": "compute_features k_min=1"},
+        "plain_ms_per_batch": round(plain_ms, 3),
+        "batched_ms_per_batch": round(batch_ms, 3),
+        "plain_points_per_s": round(n_total / plain_ms * 1e3, 1),
+        "value": round(n_total / batch_ms * 1e3, 1),
+        "unit": UNIT,
+        "speedup_batched_vs_plain": round(plain_ms / batch_ms, 2),
+        "steps": args.steps,
+        "matches_per_cloud": ok,
+    }
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "batch" and args.impl == "ours":
+        if rank == 0:
+            print(json.dumps(run_batch(args)), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference(args, rank, world)
     else:

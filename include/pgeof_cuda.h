@@ -168,6 +168,29 @@ int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xyz, const ui
                                        const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features,
                                        uint32_t* error_bits, pgeof_stream_t stream);
 
+/* ------------------------------------------------ multi-cloud batches */
+/* knn_search(cloud, cloud, knn) followed by compute_features(k_min=1) on the
+ * kNN CSR, for many clouds at once (include/nn_search.hpp:31-67 and
+ * include/pgeof.hpp:75-117 per cloud). xyz holds the clouds back to back;
+ * `offsets` is a HOST array of n_clouds + 1 row offsets (offsets[0] = 0).
+ * indices: (N, knn) uint32, local to each cloud; sqr_dist: (N, knn);
+ * features: (N, 11) or NULL. Results equal the per-cloud calls exactly.
+ * Errors: knn larger than some cloud. */
+int pgeof_batch_knn_features_f32(const float* xyz, const int64_t* offsets, int64_t n_clouds, uint32_t knn,
+                                 uint32_t* indices, float* sqr_dist, float* features, pgeof_stream_t stream);
+
+/* The same pipeline captured once into a CUDA graph for a fixed batch shape
+ * and fixed device buffers: create (tunes the grid cell size on the given
+ * data, synchronises `stream`), then launch any number of times after
+ * refilling xyz in place. No reference counterpart (the reference has no
+ * batch API). */
+typedef struct pgeof_batch_plan_s* pgeof_batch_plan;
+int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_clouds, uint32_t knn,
+                            uint32_t* indices, float* sqr_dist, float* features, pgeof_stream_t stream,
+                            pgeof_batch_plan* out);
+int pgeof_batch_plan_launch(pgeof_batch_plan plan, pgeof_stream_t stream);
+int pgeof_batch_plan_destroy(pgeof_batch_plan plan);
+
 /* ------------------------------------------------ host-pointer API (sync) */
 /* Same semantics as the device entry points above; every pointer is host
  * memory. These are what the Python drop-in binding calls for numpy inputs. */

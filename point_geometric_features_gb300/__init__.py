@@ -45,6 +45,8 @@ __all__ = [
     "get_eig_order",
     "kernel_launch_count",
     "check_device_errors",
+    "batch_knn_features",
+    "BatchPlan",
 ]
 
 
@@ -230,3 +232,77 @@ def compute_features_selected(xyz, search_radius, max_knn, selected_features):
                                                 ids, f64, out.data_ptr(), s)
         return out
     return _ext.compute_features_selected(xyz, search_radius, max_knn, selected_features)
+
+
+# --------------------------------------------------------------- multi-cloud batches
+def _batch_inputs(clouds, offsets):
+    torch = _sys.modules["torch"]
+    if isinstance(clouds, (list, tuple)):
+        offsets = [0]
+        for c in clouds:
+            _dev_cloud(c, "cloud")
+            offsets.append(offsets[-1] + int(c.shape[0]))
+        xyz = torch.cat(list(clouds), 0).contiguous()
+    else:
+        xyz = _dev_cloud(clouds, "xyz")
+        offsets = [int(v) for v in offsets]
+    return xyz, offsets
+
+
+def batch_knn_features(clouds, k, offsets=None, features=True):
+    """knn_search(cloud, cloud, k) and compute_features on its kNN CSR for many
+    clouds in one device pipeline (no host round trip between kernels).
+
+    ``clouds``: a list of contiguous CUDA float32 (n_i, 3) tensors, or one
+    (N, 3) tensor with ``offsets`` (n_clouds + 1 row offsets). Returns
+    ``(indices, sqr_dist, features)`` over all N rows: uint32 (N, k) indices
+    local to each cloud, float32 (N, k) squared distances, float32 (N, 11)
+    features (None when ``features`` is False) -- equal to the per-cloud calls.
+    """
+    torch = _sys.modules["torch"]
+    xyz, offs = _batch_inputs(clouds, offsets)
+    n = xyz.shape[0]
+    with torch.cuda.device(xyz.device):
+        s = int(torch.cuda.current_stream().cuda_stream)
+        idx = _uint32_empty(torch, (n, int(k)), xyz.device)
+        d2 = torch.empty((n, int(k)), dtype=torch.float32, device=xyz.device)
+        f = torch.empty((n, 11), dtype=torch.float32, device=xyz.device) if features else None
+        _ext._dev_batch_knn_features(xyz.data_ptr(), offs, int(k), idx.data_ptr(), d2.data_ptr(),
+                                     f.data_ptr() if f is not None else 0, s)
+    return idx, d2, f
+
+
+class BatchPlan:
+    """The batch pipeline captured once into a CUDA graph for a fixed batch
+    shape: ``plan = BatchPlan(xyz, offsets, k)``; refill ``plan.xyz`` in place
+    and call ``plan()``; results land in ``plan.indices``, ``plan.sqr_dist``,
+    ``plan.features``. Creation tunes the grid cell size on the given data."""
+
+    def __init__(self, clouds, k, offsets=None, features=True):
+        torch = _sys.modules["torch"]
+        self.xyz, self.offsets = _batch_inputs(clouds, offsets)
+        n = self.xyz.shape[0]
+        dev = self.xyz.device
+        self.indices = _uint32_empty(torch, (n, int(k)), dev)
+        self.sqr_dist = torch.empty((n, int(k)), dtype=torch.float32, device=dev)
+        self.features = torch.empty((n, 11), dtype=torch.float32, device=dev) if features else None
+        with torch.cuda.device(dev):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            self._h = _ext._batch_plan_create(self.xyz.data_ptr(), self.offsets, int(k), self.indices.data_ptr(),
+                                              self.sqr_dist.data_ptr(),
+                                              self.features.data_ptr() if features else 0, s)
+
+    def __call__(self, stream=None):
+        _ext._batch_plan_launch(self._h, _stream_handle(stream))
+        return self.indices, self.sqr_dist, self.features
+
+    def close(self):
+        if getattr(self, "_h", 0):
+            _ext._batch_plan_destroy(self._h)
+            self._h = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -40,18 +40,27 @@ struct FeatArgs {
     float* out;
     uint32_t* err;
     unsigned long long* resolved;  // neighbourhoods re-solved in double (stats)
+    // multi-cloud batches: row r belongs to the cloud c with off[c] <= r < off[c+1];
+    // its neighbour indices are local to that cloud's slice of xyz4
+    const uint64_t* cloud_off;
+    int n_clouds;
 };
 
-__device__ __forceinline__ float4 load_nb(const FeatArgs& a, uint64_t pos, uint32_t& flags) {
+struct RowCloud {
+    const float4* xyz4;
+    uint32_t n;
+};
+
+__device__ __forceinline__ float4 load_nb(const FeatArgs& a, const RowCloud& rc, uint64_t pos, uint32_t& flags) {
     uint32_t id = __ldg(a.nn + pos);
-    if (id >= a.n_xyz) {
+    if (id >= rc.n) {
         flags |= ERR_NN_RANGE;
         id = 0;
     }
-    return __ldg(a.xyz4 + id);
+    return __ldg(rc.xyz4 + id);
 }
 
-template <int S>
+template <int S, bool MULTI>
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
     extern __shared__ float stage[];  // kFeatThreads * n_scales * 11
     const int tid = threadIdx.x;
@@ -68,6 +77,17 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             flags |= ERR_PTR_RANGE;
         } else {
             k_nn = e - b;
+        }
+        RowCloud rc{a.xyz4, a.n_xyz};
+        if (MULTI) {
+            int lo = 0, hi = a.n_clouds - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.cloud_off[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            rc.xyz4 = a.xyz4 + a.cloud_off[lo];
+            rc.n = (uint32_t)(a.cloud_off[lo + 1] - a.cloud_off[lo]);
         }
         uint32_t ks[S];
         int n_active = 0;
@@ -92,7 +112,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
 #pragma unroll
             for (int s = 0; s < S; ++s) sx[s] = sy[s] = sz[s] = 0.0f;
             for (uint32_t j = 0; j < kmax; ++j) {
-                const float4 p = load_nb(a, (uint64_t)b + j, flags);
+                const float4 p = load_nb(a, rc, (uint64_t)b + j, flags);
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
                     if (s < n_active && j < ks[s]) {
@@ -115,7 +135,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
 #pragma unroll
             for (int s = 0; s < S; ++s) cxx[s] = cxy[s] = cxz[s] = cyy[s] = cyz[s] = czz[s] = 0.0f;
             for (uint32_t j = 0; j < kmax; ++j) {
-                const float4 p = load_nb(a, (uint64_t)b + j, flags);
+                const float4 p = load_nb(a, rc, (uint64_t)b + j, flags);
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
                     if (s < n_active && j < ks[s]) {
@@ -445,16 +465,20 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
     const size_t smem = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
     const unsigned blocks = ceil_div_u(a.n_points, kFeatThreads);
     KernelTimer kt("features_kernel", s);
-    features_kernel<S><<<blocks, kFeatThreads, smem, s>>>(a);
+    if (a.n_clouds > 0) features_kernel<S, true><<<blocks, kFeatThreads, smem, s>>>(a);
+    else features_kernel<S, false><<<blocks, kFeatThreads, smem, s>>>(a);
     count_launch();
     return check_launch("features_kernel");
 }
 
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
-                    float* out, unsigned long long* resolved, cudaStream_t s) {
+                    float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off,
+                    int n_clouds) {
     if (n_points == 0) return PGEOF_OK;
     FeatArgs a{};
+    a.cloud_off = cloud_off;
+    a.n_clouds = cloud_off ? n_clouds : 0;
     a.xyz4 = xyz4;
     a.n_xyz = (uint32_t)n_xyz;
     a.nn = nn;
@@ -616,7 +640,7 @@ extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xy
     a.err = err;
     a.resolved = nullptr;
     const size_t smem = (size_t)kFeatThreads * 11 * sizeof(float);
-    features_kernel<1><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
+    features_kernel<1, false><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
     count_launch();
     return check_launch("features_kernel (noalloc)");
 }

@@ -191,6 +191,10 @@ __global__ void scatter_kernel(const T* __restrict__ xyz, uint64_t n, const uint
     }
 }
 
+}  // namespace
+int exclusive_scan_into(const uint32_t* in, uint32_t G, uint32_t* out, uint32_t* partials, cudaStream_t s);
+namespace {
+
 unsigned grid_blocks(uint64_t n, int threads) {
     const DeviceInfo* di = nullptr;
     current_device_info(&di);
@@ -202,12 +206,7 @@ int exclusive_scan(const uint32_t* in, uint32_t G, uint32_t* out, cudaStream_t s
     const uint32_t nb = ceil_div_u(G, kScanTile);
     Scratch part;
     PGEOF_TRY(part.alloc((size_t)nb * sizeof(uint32_t), s));
-    KernelTimer kt("scan_kernels", s);
-    scan_partials_kernel<<<nb, kScanThreads, 0, s>>>(in, G, part.as<uint32_t>());
-    scan_top_kernel<<<1, kScanThreads, 0, s>>>(part.as<uint32_t>(), nb);
-    scan_final_kernel<<<nb, kScanThreads, 0, s>>>(in, G, part.as<uint32_t>(), out);
-    count_launch(3);
-    return check_launch("exclusive_scan");
+    return exclusive_scan_into(in, G, out, part.as<uint32_t>(), s);
 }
 
 struct HostBox {
@@ -303,6 +302,18 @@ static int occupancy(const T* xyz, uint64_t n, const GridParams& g, uint32_t* co
 }
 
 }  // namespace
+
+// Exclusive scan of G counts into out[0..G] with caller-owned partials
+// (ceil(G / 1024) words): no allocation, so it can be captured in a graph.
+int exclusive_scan_into(const uint32_t* in, uint32_t G, uint32_t* out, uint32_t* partials, cudaStream_t s) {
+    const uint32_t nb = ceil_div_u(G, kScanTile);
+    KernelTimer kt("scan_kernels", s);
+    scan_partials_kernel<<<nb, kScanThreads, 0, s>>>(in, G, partials);
+    scan_top_kernel<<<1, kScanThreads, 0, s>>>(partials, nb);
+    scan_final_kernel<<<nb, kScanThreads, 0, s>>>(in, G, partials, out);
+    count_launch(3);
+    return check_launch("exclusive_scan");
+}
 
 template <typename T>
 int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h_max, GridIndex<T>& out,

@@ -8,9 +8,12 @@ namespace pgeof {
 
 // ----------------------------------------------------------- feature passes
 int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s);
+// cloud_off (device, n_clouds + 1): rows of a multi-cloud batch, neighbour
+// indices local to each cloud's slice of xyz4 (null: one cloud).
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
-                    float* out, unsigned long long* resolved, cudaStream_t s);
+                    float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off = nullptr,
+                    int n_clouds = 0);
 int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                    uint64_t n_points, uint32_t k_min, uint32_t k_step, uint32_t k_min_search, float* out,
                    unsigned long long* stats, cudaStream_t s);
@@ -63,6 +66,28 @@ template <typename T>
 int sort_queries(const T* q, uint64_t m, const GridParams& g, Scratch& out_mem, SPoint<T>** out, Scratch& start,
                  cudaStream_t s);
 
+// Multi-cloud batches: cloud c owns points [off[c], off[c + 1]) of the
+// concatenated input and of the cell-sorted point array, and cells
+// [cell_base[c], cell_base[c] + g[c].n_cells) of the shared cell table, whose
+// entries are positions in the shared sorted array. n == 0: a single cloud.
+struct CloudTable {
+    const GridParams* g = nullptr;
+    const uint32_t* cell_base = nullptr;
+    const uint64_t* off = nullptr;
+    int n = 0;
+};
+
+// The cloud owning position `pos` (last c with off[c] <= pos).
+__device__ __forceinline__ int cloud_of(const CloudTable& ct, uint64_t pos) {
+    int lo = 0, hi = ct.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ct.off[mid] <= pos) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ----------------------------------------------------------- neighbour search
 enum SearchMode { MODE_KNN = 0, MODE_RADIUS = 1 };
 
@@ -79,6 +104,14 @@ struct SearchOut {
 template <typename T>
 int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint32_t* qstart, uint64_t m, int mode,
                   uint32_t k, T radius, const SearchOut<T>& out, cudaStream_t s);
+
+// Self-kNN over a multi-cloud batch: `pts` are all clouds' points in (cloud,
+// cell) order with cloud-local indices, `cell_start` the shared cell table;
+// output rows are global (off[c] + local index), neighbour indices local.
+// `work` points to 8 zeroed words and `ovf` to n_points words of device scratch.
+int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const SPoint<float>* pts, uint64_t n_points,
+                        uint32_t k, uint32_t* indices, float* sqr_dist, uint32_t* work, uint32_t* ovf,
+                        cudaStream_t s);
 
 // PCA + selected features from a radius-search neighbour table (selected path).
 template <typename T>

@@ -304,6 +304,31 @@ PYBIND11_MODULE(pgeof_ext, m) {
                                                        P<const uint32_t>(ptr), n, k_min, k_step, k_min_search,
                                                        P<float>(out), P<void>(stream)));
           });
+    m.def("_dev_batch_knn_features", [](uintptr_t xyz, const std::vector<int64_t>& offsets, uint32_t k, uintptr_t idx,
+                                        uintptr_t d2, uintptr_t feats, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_batch_knn_features_f32(P<const float>(xyz), offsets.data(), (int64_t)offsets.size() - 1, k,
+                                           P<uint32_t>(idx), P<float>(d2), P<float>(feats), P<void>(stream)));
+    });
+    m.def("_batch_plan_create", [](uintptr_t xyz, const std::vector<int64_t>& offsets, uint32_t k, uintptr_t idx,
+                                   uintptr_t d2, uintptr_t feats, uintptr_t stream) {
+        pgeof_batch_plan plan = nullptr;
+        int st;
+        {
+            py::gil_scoped_release nogil;
+            st = pgeof_batch_plan_create(P<const float>(xyz), offsets.data(), (int64_t)offsets.size() - 1, k,
+                                         P<uint32_t>(idx), P<float>(d2), P<float>(feats), P<void>(stream), &plan);
+        }
+        check(st);
+        return reinterpret_cast<uintptr_t>(plan);
+    });
+    m.def("_batch_plan_launch", [](uintptr_t plan, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_batch_plan_launch(reinterpret_cast<pgeof_batch_plan>(plan), P<void>(stream)));
+    });
+    m.def("_batch_plan_destroy", [](uintptr_t plan) {
+        check(pgeof_batch_plan_destroy(reinterpret_cast<pgeof_batch_plan>(plan)));
+    });
     m.def("_dev_compute_features_selected",
           [](uintptr_t xyz, int64_t n, double r, uint32_t max_knn, const std::vector<int32_t>& ids, bool f64,
              uintptr_t out, uintptr_t stream) {

@@ -97,6 +97,7 @@ struct GridView {
 template <typename T>
 struct SearchArgs {
     GridView<T> gv;
+    CloudTable ct;
     const SPoint<T>* queries;
     uint64_t m;
     const uint32_t* qlist;   // optional: positions in `queries` to process
@@ -411,17 +412,26 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
                         ? reinterpret_cast<Entry<T>*>(smem_raw + kSearchWarps * sizeof(WarpSmem<T>)) + (size_t)wib * a.cap
                         : a.gbuf + ((size_t)blockIdx.x * kSearchWarps + wib) * a.cap;
     const uint64_t nwarps = (uint64_t)gridDim.x * kSearchWarps;
-    const GridParams& g = a.gv.g;
     const uint64_t m = a.qlist ? (uint64_t)*a.qcount : a.m;
 
     for (uint64_t qi = (uint64_t)blockIdx.x * kSearchWarps + wib; qi < m; qi += nwarps) {
-        const SPoint<T> qp = a.queries[a.qlist ? a.qlist[qi] : qi];
+        const uint64_t qpos = a.qlist ? a.qlist[qi] : qi;
+        const SPoint<T> qp = a.queries[qpos];
+        GridView<T> gv = a.gv;
+        uint64_t row_base = 0;
+        if (a.ct.n) {
+            const int ci = cloud_of(a.ct, qpos);
+            gv.g = a.ct.g[ci];
+            gv.cell_start = a.gv.cell_start + a.ct.cell_base[ci];
+            row_base = a.ct.off[ci];
+        }
+        const GridParams& g = gv.g;
         const T q[3] = {qp.x, qp.y, qp.z};
         const uint32_t k = a.k;
         T tau2;
         bool strict;
         if (a.mode == MODE_KNN) {
-            tau2 = pilot_tau2<T>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
+            tau2 = pilot_tau2<T>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
             strict = false;
         } else {
             tau2 = a.r2;
@@ -447,7 +457,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
             ws->imax[lane] = 0;
             __syncwarp();
             uint32_t count = 0;
-            visit_box<T>(a.gv, ws->run_start, ws->run_len, q, rb, true, tf, [&](bool valid, T d2, uint32_t idx) {
+            visit_box<T>(gv, ws->run_start, ws->run_len, q, rb, true, tf, [&](bool valid, T d2, uint32_t idx) {
                 const bool member = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
                 const int st = member ? classify<T>(ws, nlev, d2, idx) : 2;
                 const bool take = st != 2;
@@ -521,7 +531,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
         int P = 1;
         while (P < (int)n_sel) P <<= 1;
         if (n_sel > 1) bitonic_sort<T>(buf, (int)n_sel, P);
-        emit_row<T>(a.mode, k, n_sel, found, qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
+        emit_row<T>(a.mode, k, n_sel, found, row_base + qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
                     [&](uint32_t j) { return buf[j]; });
         __syncwarp();
     }
@@ -535,6 +545,7 @@ constexpr int kMaxInBin = 24;    // larger bins (exact ties) fall back to a bito
 
 struct FastArgs {
     GridView<float> gv;
+    CloudTable ct;
     const SPoint<float>* queries;
     uint64_t m;
     int mode;
@@ -665,6 +676,7 @@ __device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* 
     __syncwarp();
 }
 
+template <bool MULTI>
 __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __grid_constant__ FastArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -672,7 +684,6 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw + kFastWarps * sizeof(FastWarpSmem)) +
                      (size_t)wib * 2 * a.cap;
     uint64_t* sorted = keys + a.cap;
-    const GridParams& g = a.gv.g;
     const uint32_t k = a.k;
     for (;;) {
         uint32_t chunk = 0;
@@ -683,8 +694,19 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
         const uint64_t q1 = min(q0 + (uint64_t)kChunk, a.m);
         // the last 32 solved queries of this chunk, one per lane: position and d_k
         float rx = 0.0f, ry = 0.0f, rz = 0.0f, rdk = -1.0f;
+        int rci = -1;
         for (uint64_t qi = q0; qi < q1; ++qi) {
             const SPoint<float> qp = a.queries[qi];
+            GridView<float> gv = a.gv;
+            uint64_t row_base = 0;
+            int ci = 0;
+            if (MULTI) {
+                ci = cloud_of(a.ct, qi);
+                gv.g = a.ct.g[ci];
+                gv.cell_start = a.gv.cell_start + a.ct.cell_base[ci];
+                row_base = a.ct.off[ci];
+            }
+            const GridParams& g = gv.g;
             const float q[3] = {qp.x, qp.y, qp.z};
             float tau2;
             bool strict;
@@ -692,7 +714,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                 strict = false;
                 // d_k(q) <= d_k(p) + |q - p| for every solved p: take the best over the lanes
                 float bound = INFINITY;
-                if (rdk >= 0.0f) {
+                if (rdk >= 0.0f && rci == ci) {
                     const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
                     const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
                     if (dq <= 0.75f * rdk) bound = rdk + dq;
@@ -702,7 +724,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                     const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
                     tau2 = t * t;
                 } else {
-                    tau2 = pilot_tau2<float>(a.gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                    tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
                 }
             } else {
                 strict = true;
@@ -711,7 +733,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             const float tf = sqrtf(tau2) * 1.000001f + g.margin;
             const Box rb = region_box(g, q[0], q[1], q[2], tf);
             uint32_t count = 0;
-            visit_box<float>(a.gv, ws->run_start, ws->run_len, q, rb, true, tf,
+            visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
                              [&](bool valid, float d2, uint32_t idx) {
                                  const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
                                  const uint32_t mask = __ballot_sync(FULL, take);
@@ -732,7 +754,8 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             }
             const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
             if (n_sel > 0) select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap);
-            emit_row<float>(a.mode, k, n_sel, count, qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
+            emit_row<float>(a.mode, k, n_sel, count, row_base + qp.idx, a.out_idx, a.out_d2, a.out_found,
+                            a.fill_last, a.r2,
                             [&](uint32_t j) {
                                 const uint64_t key = sorted[j];
                                 Entry<float> e;
@@ -745,6 +768,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                 rx = q[0];
                 ry = q[1];
                 rz = q[2];
+                rci = ci;
             }
             __syncwarp();
         }
@@ -838,9 +862,9 @@ int general_smem_bytes(uint32_t cap, bool in_smem) {
 }
 
 template <typename T>
-int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, const uint32_t* qlist,
-                   const uint32_t* qcount, int mode, uint32_t k, T radius, const SearchOut<T>& out,
-                   cudaStream_t s) {
+int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoint<T>* queries, uint64_t m,
+                        const uint32_t* qlist, const uint32_t* qcount, int mode, uint32_t k, T radius,
+                        const SearchOut<T>& out, cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     // buffer capacity: a power of two comfortably above k
@@ -861,9 +885,8 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
         PGEOF_TRY(gbuf.alloc(blocks * kSearchWarps * (size_t)cap * sizeof(Entry<T>), s));
         a.gbuf = gbuf.as<Entry<T>>();
     }
-    a.gv.g = grid.g;
-    a.gv.cell_start = grid.cell_start;
-    a.gv.pts = grid.pts;
+    a.gv = gv;
+    a.ct = ct;
     a.queries = queries;
     a.m = m;
     a.qlist = qlist;
@@ -885,6 +908,62 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
     return check_launch("search_kernel");
 }
 
+template <typename T>
+int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t m, const uint32_t* qlist,
+                   const uint32_t* qcount, int mode, uint32_t k, T radius, const SearchOut<T>& out,
+                   cudaStream_t s) {
+    GridView<T> gv;
+    gv.g = grid.g;
+    gv.cell_start = grid.cell_start;
+    gv.pts = grid.pts;
+    return launch_general_view<T>(gv, CloudTable{}, queries, m, qlist, qcount, mode, k, radius, out, s);
+}
+
+// The fast kernel over `queries` (cell order), then the general kernel over the
+// queries whose buffer overflowed. `words`: 8 zeroed words + m words.
+int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<float>* queries, uint64_t m, int mode,
+                uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, cudaStream_t s) {
+    const DeviceInfo* di;
+    PGEOF_TRY(current_device_info(&di));
+    uint32_t cap = 1;
+    const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? 256 : 512, 4ull * k);
+    while (cap < want) cap <<= 1;
+    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + 2 * (size_t)cap * sizeof(uint64_t)));
+    auto kern = ct.n ? fast_search_kernel<true> : fast_search_kernel<false>;
+    if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int per_sm = 0;
+    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastWarps * 32, smem));
+    per_sm = std::max(per_sm, 1);
+    const uint64_t chunks = ceil_div_u(m, kChunk);
+    const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
+    PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
+    FastArgs a{};
+    a.gv = gv;
+    a.ct = ct;
+    a.queries = queries;
+    a.m = m;
+    a.mode = mode;
+    a.k = k;
+    a.r2 = radius * radius;  // sq_search_radius in real_t, nn_search.hpp:98
+    a.cap = cap;
+    a.work = words;
+    a.ovf_count = words + 1;
+    a.ovf_list = words + 8;
+    a.out_idx = out.indices;
+    a.out_d2 = out.sqr_dist;
+    a.out_found = out.found;
+    a.fill_last = out.radius_fill_last ? 1 : 0;
+    a.err = device_error_word();
+    {
+        KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
+        kern<<<(unsigned)blocks, kFastWarps * 32, smem, s>>>(a);
+    }
+    count_launch();
+    PGEOF_TRY(check_launch("fast_search_kernel"));
+    // queries whose key buffer overflowed: the general kernel, sized on the device
+    return launch_general_view<float>(gv, ct, queries, m, a.ovf_list, a.ovf_count, mode, k, radius, out, s);
+}
+
 }  // namespace
 
 template <typename T>
@@ -895,53 +974,32 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
     if constexpr (sizeof(T) != sizeof(float)) {
         return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
     } else {
-    if (k > 128 || m >= 0xffffffffull)
-        return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
-    const DeviceInfo* di;
-    PGEOF_TRY(current_device_info(&di));
-    uint32_t cap = 1;
-    const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? 256 : 512, 4ull * k);
-    while (cap < want) cap <<= 1;
-    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + 2 * (size_t)cap * sizeof(uint64_t)));
-    if (smem > 48 * 1024)
-        PGEOF_CUDA_TRY(cudaFuncSetAttribute(fast_search_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    int per_sm = 0;
-    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fast_search_kernel, kFastWarps * 32, smem));
-    per_sm = std::max(per_sm, 1);
-    const uint64_t chunks = ceil_div_u(m, kChunk);
-    const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
-    // work counter, overflow count, overflow list
-    Scratch ctl;
-    PGEOF_TRY(ctl.alloc((m + 8) * sizeof(uint32_t), s));
-    uint32_t* words = ctl.as<uint32_t>();
-    PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
-    FastArgs a{};
-    a.gv.g = grid.g;
-    a.gv.cell_start = grid.cell_start;
-    a.gv.pts = reinterpret_cast<const SPoint<float>*>(grid.pts);
-    a.queries = reinterpret_cast<const SPoint<float>*>(queries);
-    a.m = m;
-    a.mode = mode;
-    a.k = k;
-    a.r2 = (float)(radius * radius);  // sq_search_radius in real_t, nn_search.hpp:98
-    a.cap = cap;
-    a.work = words;
-    a.ovf_count = words + 1;
-    a.ovf_list = words + 8;
-    a.out_idx = out.indices;
-    a.out_d2 = reinterpret_cast<float*>(out.sqr_dist);
-    a.out_found = out.found;
-    a.fill_last = out.radius_fill_last ? 1 : 0;
-    a.err = device_error_word();
-    {
-        KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
-        fast_search_kernel<<<(unsigned)blocks, kFastWarps * 32, smem, s>>>(a);
+        if (k > 128 || m >= 0xffffffffull)
+            return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
+        Scratch ctl;
+        PGEOF_TRY(ctl.alloc((m + 8) * sizeof(uint32_t), s));
+        GridView<float> gv;
+        gv.g = grid.g;
+        gv.cell_start = grid.cell_start;
+        gv.pts = grid.pts;
+        return launch_fast(gv, CloudTable{}, queries, m, mode, k, radius, out, ctl.as<uint32_t>(), s);
     }
-    count_launch();
-    PGEOF_TRY(check_launch("fast_search_kernel"));
-    // queries whose buffer overflowed: the general kernel, sized on the device
-    return launch_general<T>(grid, queries, m, a.ovf_list, a.ovf_count, mode, k, radius, out, s);
-    }
+}
+
+int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const SPoint<float>* pts, uint64_t n_points,
+                        uint32_t k, uint32_t* indices, float* sqr_dist, uint32_t* work, uint32_t* ovf,
+                        cudaStream_t s) {
+    if (n_points == 0 || k == 0) return PGEOF_OK;
+    GridView<float> gv{};
+    gv.cell_start = cell_start;
+    gv.pts = pts;
+    SearchOut<float> out;
+    out.indices = indices;
+    out.sqr_dist = sqr_dist;
+    if (k > 128)
+        return launch_general_view<float>(gv, ct, pts, n_points, nullptr, nullptr, MODE_KNN, k, 0.0f, out, s);
+    (void)ovf;
+    return launch_fast(gv, ct, pts, n_points, MODE_KNN, k, 0.0f, out, work, s);
 }
 
 template <typename T>
