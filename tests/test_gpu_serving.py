@@ -1,0 +1,54 @@
+"""Serving (configs[4] shape, scaled down): requests admitted while others run
+overlap on the GPU, and every result equals the same request run alone."""
+
+import numpy as np
+import pytest
+
+from point_geometric_features_gb300.synthetic import log_uniform_sizes, scaled_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _pool(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    sizes = log_uniform_sizes(n, lo, hi, seed)
+    return [scaled_scene(int(s), seed=seed * 100 + i, side=float(rng.uniform(5.0, 50.0))) for i, s in enumerate(sizes)]
+
+
+def test_results_same_alone_and_in_the_mix(cuda, pgeof):
+    from point_geometric_features_gb300.serving import Request, Server, radius_for_count
+
+    pool = _pool(10, 1_000, 60_000, seed=5)
+    rng = np.random.default_rng(6)
+    feats = [pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z]
+    reqs = []
+    for i in range(30):
+        xyz = pool[int(rng.integers(len(pool)))]
+        k = int(rng.choice([16, 32, 64]))
+        reqs.append(Request(i, xyz, k, radius_for_count(xyz, 1.5 * k), feats))
+    alone = {r.rid: pgeof.compute_features_selected(r.xyz, r.radius, r.max_knn, feats) for r in reqs}
+    server = Server(slots=4, budget_bytes=2 << 30)
+    try:
+        for r in reqs:  # a burst: many in flight at once
+            server.submit(r)
+        results = server.drain(len(reqs), timeout=300)
+    finally:
+        server.close()
+    assert server.adm.peak_in_flight > 1  # work really overlapped
+    assert len({r.slot for r in results}) > 1
+    for res in results:
+        np.testing.assert_array_equal(res.features, alone[res.rid])
+
+
+def test_poisson_stream_summary(cuda, pgeof):
+    from point_geometric_features_gb300.serving import Server, run_stream
+
+    pool = _pool(8, 1_000, 50_000, seed=7)
+    server = Server(slots=4, budget_bytes=4 << 30)
+    try:
+        out = run_stream(server, pool, rate=60.0, duration=2.0, seed=8)
+    finally:
+        server.close()
+    assert out["requests"] > 60
+    assert 0 < out["p50_ms"] <= out["p99_ms"] < 5_000
+    assert out["points_per_s"] > 0
