@@ -61,7 +61,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
-    p.add_argument("--workload", choices=["scene", "batch", "serve"], default="scene",
+    p.add_argument("--workload", choices=["scene", "batch", "serve", "optimal"], default="scene",
                    help="scene: the headline 1M-point kNN+multiscale step; batch: 256 clouds, plain vs batched; "
                         "serve: Poisson request stream with p50/p99 latency")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
@@ -507,9 +507,58 @@ def run_serve(args):
     }
 
 
+def run_optimal(args):
+    """configs[2]: the 4,000,000-point outdoor scene (seed 2), radius_search
+    r = 0.5 m, max_knn = 64 -> CSR on the device (mask -1) ->
+    compute_features_optimal(k_min=1, k_step=1, k_min_search=10). Per-feature
+    errors against the FP64 oracle are measured by tests/test_gpu_accuracy.py."""
+    import torch
+
+    import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    torch.cuda.set_device(0)
+    n = 4_000_000
+    t = torch.from_numpy(outdoor_scene(n, seed=2)).cuda()
+
+    def step():
+        idx, _ = pgeof.radius_search(t, t, 0.5, 64)
+        mask = idx >= 0
+        ptr = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
+        ptr[1:] = torch.cumsum(mask.sum(1, dtype=torch.int32), 0, dtype=torch.int32)
+        nn = idx[mask]
+        return pgeof.compute_features_optimal(t, nn, ptr, 1, 1, 10, check=False)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    pgeof.profile_kernels(True)
+    pgeof.kernel_profile()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        out = step()
+    e1.record()
+    torch.cuda.synchronize()
+    prof = pgeof.kernel_profile()
+    pgeof.profile_kernels(False)
+    ms = e0.elapsed_time(e1) / args.steps
+    return {
+        "metric": METRIC, "workload": "optimal",
+        "config": {"points": n, "radius": 0.5, "max_knn": 64, "k_min": 1, "k_step": 1, "k_min_search": 10},
+        "ms_per_step": round(ms, 3), "value": round(n / ms * 1e3, 1), "unit": UNIT, "steps": args.steps,
+        "kernels": {k: {"launches": v[0], "ms_per_step": round(v[1] / args.steps, 4)} for k, v in prof.items()},
+        "k_opt_mean": float(out[:, 11][out[:, 11] > 0].mean().item()),
+    }
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "optimal" and args.impl == "ours":
+        if rank == 0:
+            print(json.dumps(run_optimal(args)), flush=True)
+        return
     if args.workload == "serve" and args.impl == "ours":
         if rank == 0:
             print(json.dumps(run_serve(args)), flush=True)
