@@ -61,9 +61,10 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
-    p.add_argument("--workload", choices=["scene", "batch", "serve", "optimal"], default="scene",
-                   help="scene: the headline 1M-point kNN+multiscale step; batch: 256 clouds, plain vs batched; "
-                        "serve: Poisson request stream with p50/p99 latency")
+    p.add_argument("--workload", choices=["scene", "features", "batch", "serve", "optimal"], default="scene",
+                   help="scene: the headline 1M-point kNN+multiscale step; features: the 1M-point k=50 "
+                        "compute_features pass alone; batch: 256 clouds, plain vs batched; serve: Poisson request "
+                        "stream with p50/p99 latency; optimal: 4M-point radius -> optimal-k")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
     return p.parse_args()
@@ -85,9 +86,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "knn_search_kernel_1M_k50.md")
+def traffic_from_profile(kernel="knn_search_kernel"):
+    """DRAM bytes per launch of `kernel` on its 1M-point k=50 workload, from the
+    committed ncu summary (profiles/<kernel>_1M_k50.md)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_1M_k50.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -552,9 +554,64 @@ def run_optimal(args):
     }
 
 
+def run_features(args):
+    """The 1M-point k=50 feature pass: compute_features over a k=50 kNN CSR of
+    the outdoor scene (the neighbour lists are built once, outside the timed
+    region), with the L2 flushed between steps. Roofline bytes per point:
+    nn (4k) + nn_ptr (4) + own xyz (12) + 11 float features (44) = 260."""
+    import torch
+
+    import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    torch.cuda.set_device(0)
+    t = torch.from_numpy(outdoor_scene(N_POINTS, seed=1)).cuda()
+    idx, _ = pgeof.knn_search(t, t, K)
+    nn = idx.view(-1)
+    ptr = torch.arange(0, K * (N_POINTS + 1), K, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(args.warmup, 3)):
+        out = pgeof.compute_features(t, nn, ptr, check=False)
+    torch.cuda.synchronize()
+    pgeof.profile_kernels(True)
+    pgeof.kernel_profile()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record()
+        out = pgeof.compute_features(t, nn, ptr, check=False)
+        stops[i].record()
+    torch.cuda.synchronize()
+    prof = pgeof.kernel_profile()
+    pgeof.profile_kernels(False)
+    pgeof.check_device_errors()
+    assert out.shape == (N_POINTS, 11) and bool(torch.isfinite(out).all())
+    ms = sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / args.steps
+    n, kms = prof.get("features_kernel", (args.steps, ms * args.steps))
+    per_launch_ms = kms / n
+    algo = 4 * K + 4 + 12 + 44
+    peak, peak_kind = measured_peaks()
+    achieved = algo * N_POINTS / (per_launch_ms / 1e3) / 1e9
+    return {
+        "metric": "points/s compute_features, 1M pts k=50", "workload": "features", "value": round(N_POINTS / ms * 1e3, 1),
+        "unit": UNIT, "ms_per_step": round(ms, 4), "steps": args.steps, "dtype": "f32",
+        "config": {"workload": "1M-point outdoor scene, compute_features over knn k=50 CSR", "points": N_POINTS,
+                   "k": K, "l2": "flushed (256 MB write) between timed steps"},
+        "roofline": {"kernel": "features_kernel", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": algo * N_POINTS, "avg_launch_ms": round(per_launch_ms, 4),
+                     "traffic": traffic_from_profile("features_kernel")},
+    }
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload == "features" and args.impl == "ours":
+        if rank == 0:
+            print(json.dumps(run_features(args)), flush=True)
+        return
     if args.workload == "optimal" and args.impl == "ours":
         if rank == 0:
             print(json.dumps(run_optimal(args)), flush=True)
