@@ -71,10 +71,9 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from point_geometric_features_gb300.replicas import dist_env as env
+
+    return env()
 
 
 def measured_peaks():
@@ -167,6 +166,7 @@ def run_ours(args, rank, world, local):
     import torch
 
     import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.replicas import max_over_ranks
     from point_geometric_features_gb300.synthetic import outdoor_scene
 
     torch.cuda.set_device(local)
@@ -222,13 +222,7 @@ def run_ours(args, rank, world, local):
     pgeof.profile_kernels(False)
     launches = pgeof.kernel_launch_count() - launches0
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, stops))
-    total_ms = ms
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(ms, device=dev)
     pgeof.check_device_errors()
     assert out.shape == (N_POINTS, len(SCALES), 11) and bool(torch.isfinite(out).all())
 
@@ -251,12 +245,7 @@ def run_ours(args, rank, world, local):
         for _ in range(e2e_steps):
             res = e2e_step()
         e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(e2e_s, device=dev)
     clk = clocks.stop()
     assert res.shape == (N_POINTS, len(SCALES), 11)
     h2d = xyz.nbytes + xyz.nbytes + N_POINTS * K * 4 + (N_POINTS + 1) * 4
