@@ -11,7 +11,7 @@
 // distance order by index (nanoflann keeps its tree-traversal order there).
 //
 // Two kernels:
-//  * fast_search_kernel (float, k <= 128): a warp takes chunks of 32
+//  * fast_search_kernel (float, k <= 128): a warp takes chunks of 16
 //    consecutive queries in cell order. One pass over the cells within a bound
 //    tau of the query appends every point with d^2 <= tau^2 to a shared-memory
 //    buffer; selection then runs in shared memory (64-bin distance histogram,
@@ -539,7 +539,11 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
 
 // ------------------------------------------------------------------ fast (float)
 constexpr int kFastWarps = 4;
-constexpr int kChunk = 64;       // consecutive queries per work item
+// Consecutive queries per work item. Small items keep the warps' finishing
+// times even: per-query cost varies several-fold across a scene (walls and
+// cylinders vs open ground), and with 64-query items the last items left warps
+// idle for a quarter of the kernel.
+constexpr int kChunk = 16;
 constexpr int kSelBins = 64;     // selection histogram
 constexpr int kMaxInBin = 24;    // larger bins (exact ties) fall back to a bitonic sort
 
