@@ -239,7 +239,8 @@ def run_ours(args, rank, world, local):
         res = out.cpu().numpy()
         e2e_s = float("nan")
     else:
-        e2e_step()
+        for _ in range(2):  # two calls: results of call i are alive during call i + 1
+            res = e2e_step()
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -293,7 +294,7 @@ def run_ours(args, rank, world, local):
                    "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(world * N_POINTS * e2e_steps / e2e_s, 1) if e2e_steps else None, "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "path": "numpy drop-in API (pageable host arrays)", "steps": e2e_steps},
+                "path": "numpy drop-in API (pageable host inputs, results in the library's cached page-locked blocks)", "steps": e2e_steps},
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roofline,

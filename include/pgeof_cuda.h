@@ -94,6 +94,19 @@ int pgeof_profile_report(char* buf, size_t buf_len);
  * bits recorded since the last call (bit 0: nn index out of range, bit 1:
  * nn_ptr not monotone or beyond len(nn), bit 2: internal bound exceeded). */
 int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits);
+/* Pinned host buffers for result arrays (no reference counterpart: the
+ * reference returns freshly allocated arrays). Writing a result into freshly
+ * mapped pageable memory costs a page fault per page, several times the copy
+ * itself; these blocks are page-locked once and cached, so a binding that
+ * backs its result arrays with them receives results at DMA speed.
+ * pgeof_host_alloc returns a block of at least `bytes` (2 MiB granules) from the
+ * cache or a new cudaHostAlloc; pgeof_host_free returns it to the cache, which
+ * keeps at most PGEOF_HOST_POOL_BYTES (environment, default 8 GiB; 0 disables
+ * caching) and releases blocks beyond that. pgeof_host_pool_trim releases every
+ * cached block. Thread-safe. */
+int pgeof_host_alloc(size_t bytes, void** ptr);
+int pgeof_host_free(void* ptr);
+int pgeof_host_pool_trim(void);
 
 /* ------------------------------------------------ device-pointer API (async) */
 

@@ -3,8 +3,11 @@
 // (memory pool, data-error word), the asynchronous device-pointer family and
 // the synchronous host-pointer family that the Python binding uses.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <unordered_map>
 #include <string>
 #include <vector>
 
@@ -337,6 +340,28 @@ int host_selected(const T* xyz, int64_t n, T radius, uint32_t max_knn, const int
     return finish_host(ce, s);
 }
 
+// Cache of page-locked host blocks behind pgeof_host_alloc / pgeof_host_free.
+struct HostPool {
+    std::mutex mu;
+    std::multimap<size_t, void*> free_blocks;  // size -> block
+    std::unordered_map<void*, size_t> size_of;  // every block handed out or cached
+    size_t cached = 0;
+    size_t cap = 0;
+    bool cap_read = false;
+};
+HostPool& host_pool() {
+    static HostPool* p = new HostPool();  // never destroyed: blocks may outlive static teardown
+    return *p;
+}
+size_t host_pool_cap(HostPool& hp) {
+    if (!hp.cap_read) {
+        hp.cap = (size_t)8 << 30;
+        if (const char* e = getenv("PGEOF_HOST_POOL_BYTES")) hp.cap = (size_t)strtoull(e, nullptr, 10);
+        hp.cap_read = true;
+    }
+    return hp.cap;
+}
+
 }  // namespace
 
 // =========================================================================
@@ -432,6 +457,71 @@ int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits) {
     PGEOF_CUDA_TRY(cudaMemcpy(&v, st->err_word, sizeof(v), cudaMemcpyDeviceToHost));
     PGEOF_CUDA_TRY(cudaMemset(st->err_word, 0, sizeof(v)));
     if (bits) *bits = v;
+    return PGEOF_OK;
+}
+
+// ---------------------------------------------------------------- host block cache
+
+int pgeof_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(PGEOF_ERR_INVALID_ARGUMENT, "pgeof_host_alloc: ptr is NULL");
+    *ptr = nullptr;
+    constexpr size_t kGranule = (size_t)2 << 20;
+    const size_t want = (std::max<size_t>(bytes, 1) + kGranule - 1) / kGranule * kGranule;
+    HostPool& hp = host_pool();
+    {
+        std::lock_guard<std::mutex> lk(hp.mu);
+        auto it = hp.free_blocks.lower_bound(want);
+        if (it != hp.free_blocks.end() && it->first <= want + want / 4) {
+            *ptr = it->second;
+            hp.cached -= it->first;
+            hp.free_blocks.erase(it);
+            return PGEOF_OK;
+        }
+    }
+    DevState* st;
+    PGEOF_TRY(device_state(&st));
+    void* p = nullptr;
+    PGEOF_CUDA_TRY(cudaHostAlloc(&p, want, cudaHostAllocPortable));
+    std::lock_guard<std::mutex> lk(hp.mu);
+    hp.size_of[p] = want;
+    *ptr = p;
+    return PGEOF_OK;
+}
+
+int pgeof_host_free(void* ptr) {
+    if (!ptr) return PGEOF_OK;
+    HostPool& hp = host_pool();
+    bool release = false;
+    {
+        std::lock_guard<std::mutex> lk(hp.mu);
+        auto it = hp.size_of.find(ptr);
+        if (it == hp.size_of.end()) return fail(PGEOF_ERR_INVALID_ARGUMENT, "pgeof_host_free: not a pgeof host block");
+        const size_t sz = it->second;
+        if (hp.cached + sz <= host_pool_cap(hp)) {
+            hp.free_blocks.emplace(sz, ptr);
+            hp.cached += sz;
+        } else {
+            hp.size_of.erase(it);
+            release = true;
+        }
+    }
+    if (release) PGEOF_CUDA_TRY(cudaFreeHost(ptr));
+    return PGEOF_OK;
+}
+
+int pgeof_host_pool_trim(void) {
+    HostPool& hp = host_pool();
+    std::vector<void*> out;
+    {
+        std::lock_guard<std::mutex> lk(hp.mu);
+        for (auto& kv : hp.free_blocks) {
+            out.push_back(kv.second);
+            hp.size_of.erase(kv.second);
+        }
+        hp.free_blocks.clear();
+        hp.cached = 0;
+    }
+    for (void* p : out) PGEOF_CUDA_TRY(cudaFreeHost(p));
     return PGEOF_OK;
 }
 

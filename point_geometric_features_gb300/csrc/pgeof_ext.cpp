@@ -9,7 +9,11 @@
 //     TypeError instead of being cast (src/pgeof_ext.cpp:34-35);
 //   * std::invalid_argument conditions raise ValueError with the reference's
 //     messages;
-//   * outputs are freshly allocated numpy arrays owned by Python.
+//   * outputs are numpy arrays owned by Python. Their memory is a page-locked
+//     block from the library's host cache (pgeof_host_alloc), returned to the
+//     cache when the array is freed, so results arrive at DMA speed instead of
+//     page-faulting fresh memory; PGEOF_HOST_POOL_BYTES=0 selects plain numpy
+//     allocations.
 // Differences: the GIL is released while the GPU works, and invalid CSR input
 // (an nn index >= len(xyz), a decreasing nn_ptr) raises ValueError where the
 // reference reads out of bounds.
@@ -20,7 +24,9 @@
 #include <pybind11/pybind11.h>
 #include <pybind11/stl.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -52,6 +58,27 @@ inline void check(int st) {
     if (st != PGEOF_OK) raise_status(st);
 }
 
+bool use_host_cache() {
+    static const bool on = [] {
+        const char* e = getenv("PGEOF_HOST_POOL_BYTES");
+        return !(e && strtoull(e, nullptr, 10) == 0);
+    }();
+    return on;
+}
+
+// A C-contiguous result array of `shape`, backed by a cached page-locked block.
+template <typename T>
+py::array_t<T, py::array::c_style> result_array(std::vector<int64_t> shape) {
+    size_t count = 1;
+    for (int64_t d : shape) count *= (size_t)std::max<int64_t>(d, 0);
+    void* p = nullptr;
+    if (count > 0 && use_host_cache() && pgeof_host_alloc(count * sizeof(T), &p) == PGEOF_OK) {
+        py::capsule owner(p, [](void* q) { pgeof_host_free(q); });
+        return py::array_t<T, py::array::c_style>(shape, static_cast<T*>(p), owner);
+    }
+    return py::array_t<T, py::array::c_style>(shape);
+}
+
 template <typename T>
 int64_t cloud_rows(const py::array_t<T, py::array::c_style>& a, const char* name) {
     if (a.ndim() != 2 || a.shape(1) != 3)
@@ -73,7 +100,7 @@ f32arr compute_features(const f32arr& xyz, const u32arr& nn, const u32arr& nn_pt
     const int64_t n_xyz = cloud_rows(xyz, "xyz");
     const int64_t nnz = vec_len(nn, "nn"), np1 = vec_len(nn_ptr, "nn_ptr");
     const int64_t n = np1 - 1;
-    f32arr out({std::max<int64_t>(n, 0), (int64_t)11});
+    f32arr out = result_array<float>({std::max<int64_t>(n, 0), (int64_t)11});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -90,7 +117,7 @@ f32arr compute_features_multiscale(const f32arr& xyz, const u32arr& nn, const u3
     const int64_t n_xyz = cloud_rows(xyz, "xyz");
     const int64_t nnz = vec_len(nn, "nn"), np1 = vec_len(nn_ptr, "nn_ptr");
     const int64_t n = np1 - 1;
-    f32arr out({std::max<int64_t>(n, 0), (int64_t)k_scales.size(), (int64_t)11});
+    f32arr out = result_array<float>({std::max<int64_t>(n, 0), (int64_t)k_scales.size(), (int64_t)11});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -107,7 +134,7 @@ f32arr compute_features_optimal(const f32arr& xyz, const u32arr& nn, const u32ar
     const int64_t n_xyz = cloud_rows(xyz, "xyz");
     const int64_t nnz = vec_len(nn, "nn"), np1 = vec_len(nn_ptr, "nn_ptr");
     const int64_t n = np1 - 1;
-    f32arr out({std::max<int64_t>(n, 0), (int64_t)12});
+    f32arr out = result_array<float>({std::max<int64_t>(n, 0), (int64_t)12});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -121,8 +148,8 @@ f32arr compute_features_optimal(const f32arr& xyz, const u32arr& nn, const u32ar
 
 std::pair<u32arr, f32arr> knn_search(const f32arr& data, const f32arr& query, uint32_t knn) {
     const int64_t n = cloud_rows(data, "data"), m = cloud_rows(query, "query");
-    u32arr idx({m, (int64_t)knn});
-    f32arr d2({m, (int64_t)knn});
+    u32arr idx = result_array<uint32_t>({m, (int64_t)knn});
+    f32arr d2 = result_array<float>({m, (int64_t)knn});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -135,8 +162,8 @@ std::pair<u32arr, f32arr> knn_search(const f32arr& data, const f32arr& query, ui
 std::pair<py::array_t<int32_t>, f32arr> radius_search(const f32arr& data, const f32arr& query, float search_radius,
                                                        uint32_t max_knn) {
     const int64_t n = cloud_rows(data, "data"), m = cloud_rows(query, "query");
-    py::array_t<int32_t> idx({m, (int64_t)max_knn});
-    f32arr d2({m, (int64_t)max_knn});
+    py::array_t<int32_t> idx = result_array<int32_t>({m, (int64_t)max_knn});
+    f32arr d2 = result_array<float>({m, (int64_t)max_knn});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -158,7 +185,7 @@ f64arr selected_f64(const f64arr& xyz, double search_radius, uint32_t max_knn,
                     const std::vector<pgeof_feature_id>& selected) {
     const int64_t n = cloud_rows(xyz, "xyz");
     const std::vector<int32_t> ids = id_list(selected);
-    f64arr out({n, (int64_t)ids.size()});
+    f64arr out = result_array<double>({n, (int64_t)ids.size()});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -173,7 +200,7 @@ f32arr selected_f32(const f32arr& xyz, float search_radius, uint32_t max_knn,
                     const std::vector<pgeof_feature_id>& selected) {
     const int64_t n = cloud_rows(xyz, "xyz");
     const std::vector<int32_t> ids = id_list(selected);
-    f32arr out({n, (int64_t)ids.size()});
+    f32arr out = result_array<float>({n, (int64_t)ids.size()});
     int st;
     {
         py::gil_scoped_release nogil;
@@ -243,6 +270,7 @@ PYBIND11_MODULE(pgeof_ext, m) {
 
     // ---- library controls
     m.def("_abi_version", &pgeof_abi_version);
+    m.def("_host_pool_trim", [] { check(pgeof_host_pool_trim()); });
     m.def("_launch_count", []() { return (uint64_t)pgeof_kernel_launch_count(); });
     m.def("_set_eig_order", [](int order) { check(pgeof_set_eig_order(order)); });
     m.def("_get_eig_order", &pgeof_get_eig_order);

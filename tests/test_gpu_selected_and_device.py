@@ -120,3 +120,27 @@ def test_kernels_actually_launch(cuda, pgeof):
     xyz = uniform_cube(1000, seed=1)
     pgeof.knn_search(xyz, xyz, 8)
     assert pgeof.kernel_launch_count() > before
+
+
+def test_result_arrays_reuse_cached_host_blocks(cuda, pgeof):
+    """Numpy results live in cached page-locked blocks: values are unaffected
+    by reuse, a block is only recycled after its array is freed, and trimming
+    the cache leaves live arrays intact."""
+    xyz = uniform_cube(20_000, seed=9)
+    i1, d1 = pgeof.knn_search(xyz, xyz, 16)
+    keep_i, keep_d = i1.copy(), d1.copy()
+    i2, d2 = pgeof.knn_search(xyz, xyz, 16)  # i1/d1 still alive: different blocks
+    assert i1.ctypes.data != i2.ctypes.data
+    np.testing.assert_array_equal(i2, keep_i)
+    del i2, d2
+    pgeof.pgeof_ext._host_pool_trim()  # releases the freed blocks only
+    np.testing.assert_array_equal(i1, keep_i)
+    np.testing.assert_array_equal(d1, keep_d)
+    for _ in range(3):
+        i3, d3 = pgeof.knn_search(xyz, xyz, 16)
+        np.testing.assert_array_equal(i3, keep_i)
+        np.testing.assert_array_equal(d3, keep_d)
+    ptr = (np.arange(xyz.shape[0] + 1) * 16).astype(np.uint32)
+    f = pgeof.compute_features(xyz, i1.reshape(-1), ptr)
+    assert f.flags.c_contiguous and f.flags.writeable and f.shape == (20_000, 11)
+    f[:] = 0  # writable like a fresh numpy array
