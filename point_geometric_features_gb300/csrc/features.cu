@@ -6,9 +6,13 @@
 // first sweep forms the float mean, the second the centred float products, the
 // exact operation order of include/pca.hpp:75-76 (Eigen's column sums run
 // sequentially), so the covariance is the one the reference forms. Multiscale
-// keeps one accumulator set per scale and fills every scale prefix in the same
-// two sweeps (the reference re-gathers each prefix). Output rows are staged in
-// shared memory and leave the block as one coalesced slab.
+// fills every scale prefix in the same two sweeps (the reference re-gathers
+// each prefix): the first keeps one running sum and takes each scale's mean
+// after that scale's last neighbour -- the value the reference's own sum over
+// the prefix produces -- the second keeps one product accumulator set per
+// scale; the scales' covariances then wait in shared memory and one copy of
+// the eigen solver handles them in turn. Output rows are staged in shared
+// memory and leave the block as one coalesced slab.
 #include <algorithm>
 #include <mutex>
 #include <string>
@@ -107,28 +111,35 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             }
         }
         if (n_active > 0) {
-            // sweep 1: sequential float sums -> means
-            float sx[S], sy[S], sz[S];
+            // sweep 1: one sequential float sum over the neighbours; every scale
+            // is a prefix of the same list summed from the first neighbour, so
+            // its sum is this running sum after its last neighbour
+            float rx = 0.0f, ry = 0.0f, rz = 0.0f;
+            float mx[S], my[S], mz[S];
 #pragma unroll
-            for (int s = 0; s < S; ++s) sx[s] = sy[s] = sz[s] = 0.0f;
+            for (int s = 0; s < S; ++s) mx[s] = my[s] = mz[s] = 0.0f;
             for (uint32_t j = 0; j < kmax; ++j) {
                 const float4 p = load_nb(a, rc, (uint64_t)b + j, flags);
+                rx = FADD(rx, p.x);
+                ry = FADD(ry, p.y);
+                rz = FADD(rz, p.z);
+                if constexpr (S > 1) {
 #pragma unroll
-                for (int s = 0; s < S; ++s) {
-                    if (s < n_active && j < ks[s]) {
-                        sx[s] = FADD(sx[s], p.x);
-                        sy[s] = FADD(sy[s], p.y);
-                        sz[s] = FADD(sz[s], p.z);
+                    for (int s = 0; s < S; ++s) {
+                        if (s < n_active && j + 1 == ks[s]) {
+                            const float kk = (float)ks[s];
+                            mx[s] = FDIV(rx, kk);
+                            my[s] = FDIV(ry, kk);
+                            mz[s] = FDIV(rz, kk);
+                        }
                     }
                 }
             }
-            float mx[S], my[S], mz[S];
-#pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const float kk = (float)ks[s];
-                mx[s] = FDIV(sx[s], kk);
-                my[s] = FDIV(sy[s], kk);
-                mz[s] = FDIV(sz[s], kk);
+            if constexpr (S == 1) {
+                const float kk = (float)ks[0];
+                mx[0] = FDIV(rx, kk);
+                my[0] = FDIV(ry, kk);
+                mz[0] = FDIV(rz, kk);
             }
             // sweep 2: centred products, sequential sums
             float cxx[S], cxy[S], cxz[S], cyy[S], cyz[S], czz[S];
@@ -151,17 +162,49 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                     }
                 }
             }
+            if constexpr (S == 1) {
+                const float kk = (float)ks[0];
+                Cov<float> c;
+                c.xx = FDIV(cxx[0], kk);
+                c.xy = FDIV(cxy[0], kk);
+                c.xz = FDIV(cxz[0], kk);
+                c.yy = FDIV(cyy[0], kk);
+                c.yz = FDIV(cyz[0], kk);
+                c.zz = FDIV(czz[0], kk);
+                Pca<float> p;
+                bool res;
+                pca_solve_f32(c, a.order, p, res);
+                n_resolved += res;
+                float f[11];
+                features11(p, f);
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-                if (s < n_active) {
-                    const float kk = (float)ks[s];
+                for (int q = 0; q < 11; ++q) stage[q * kFeatThreads + tid] = f[q];
+            } else {
+                // park each scale's covariance in its staging slot, then solve the
+                // scales one at a time (one copy of the solver, not S)
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    if (s < n_active) {
+                        const float kk = (float)ks[s];
+                        float* st = stage + (s * 11) * kFeatThreads + tid;
+                        st[0 * kFeatThreads] = FDIV(cxx[s], kk);
+                        st[1 * kFeatThreads] = FDIV(cxy[s], kk);
+                        st[2 * kFeatThreads] = FDIV(cxz[s], kk);
+                        st[3 * kFeatThreads] = FDIV(cyy[s], kk);
+                        st[4 * kFeatThreads] = FDIV(cyz[s], kk);
+                        st[5 * kFeatThreads] = FDIV(czz[s], kk);
+                    }
+                }
+#pragma unroll 1
+                for (int s = 0; s < n_active; ++s) {
+                    float* st = stage + (s * 11) * kFeatThreads + tid;
                     Cov<float> c;
-                    c.xx = FDIV(cxx[s], kk);
-                    c.xy = FDIV(cxy[s], kk);
-                    c.xz = FDIV(cxz[s], kk);
-                    c.yy = FDIV(cyy[s], kk);
-                    c.yz = FDIV(cyz[s], kk);
-                    c.zz = FDIV(czz[s], kk);
+                    c.xx = st[0 * kFeatThreads];
+                    c.xy = st[1 * kFeatThreads];
+                    c.xz = st[2 * kFeatThreads];
+                    c.yy = st[3 * kFeatThreads];
+                    c.yz = st[4 * kFeatThreads];
+                    c.zz = st[5 * kFeatThreads];
                     Pca<float> p;
                     bool res;
                     pca_solve_f32(c, a.order, p, res);
@@ -169,7 +212,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                     float f[11];
                     features11(p, f);
 #pragma unroll
-                    for (int q = 0; q < 11; ++q) stage[(s * 11 + q) * kFeatThreads + tid] = f[q];
+                    for (int q = 0; q < 11; ++q) st[q * kFeatThreads] = f[q];
                 }
             }
         }
@@ -507,7 +550,9 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
         int st;
         if (cnt == 1) st = launch_features_s<1>(a, s);
         else if (cnt == 2) st = launch_features_s<2>(a, s);
-        else if (cnt <= 4) st = launch_features_s<4>(a, s);
+        else if (cnt == 3) st = launch_features_s<3>(a, s);
+        else if (cnt == 4) st = launch_features_s<4>(a, s);
+        else if (cnt <= 6) st = launch_features_s<6>(a, s);
         else st = launch_features_s<8>(a, s);
         if (st != PGEOF_OK) return st;
     }
