@@ -555,7 +555,8 @@ struct FastArgs {
     int mode;
     uint32_t k;
     float r2;
-    uint32_t cap;  // power of two, buffer entries per warp
+    uint32_t cap;         // power of two, candidate keys per warp
+    uint32_t cap_sorted;  // power of two, selected keys per warp
     uint32_t* work;
     uint32_t* ovf_list;
     uint32_t* ovf_count;
@@ -599,11 +600,12 @@ __device__ __forceinline__ void bitonic_keys(uint64_t* keys, int n, int P) {
     }
 }
 
-// Sort the n_sel smallest of keys[0..count) into out[0..n_sel) (count <= cap,
-// every key has d^2 <= tau2). Returns nothing; out is fully ordered up to the
-// last bin that contains the n_sel-th key.
-__device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* keys, uint32_t count,
-                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t cap) {
+// Sort the n_sel smallest of keys[0..count) into out (every key has d^2 <=
+// tau2): out is fully ordered up to the last bin that contains the n_sel-th
+// key. Returns false, writing nothing, when those bins hold more than out_cap
+// keys.
+__device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* keys, uint32_t count,
+                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t out_cap) {
     const int lane = threadIdx.x & 31;
     const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
     ws->hist[lane] = 0;
@@ -644,6 +646,7 @@ __device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* 
                        hh1 = __shfl_sync(FULL, h1, lb);
         n_take = (bstar & 1) ? e + hh0 + hh1 : e + hh0;
     }
+    if (n_take > out_cap) return false;
     for (uint32_t i = lane; i < count; i += 32) {
         const uint64_t key = keys[i];
         const float x = key_d2(key) * sb;
@@ -655,9 +658,10 @@ __device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* 
         // exact ties crowd a bin: sort the whole prefix
         int P = 1;
         while (P < (int)n_take) P <<= 1;
-        if (P <= (int)cap) bitonic_keys(out, (int)n_take, P);
+        if (P > (int)out_cap) return false;
+        bitonic_keys(out, (int)n_take, P);
         __syncwarp();
-        return;
+        return true;
     }
     // insertion sort inside each bin (a handful of keys each)
 #pragma unroll
@@ -678,6 +682,7 @@ __device__ __forceinline__ void select_sorted(FastWarpSmem* ws, const uint64_t* 
         }
     }
     __syncwarp();
+    return true;
 }
 
 template <bool MULTI>
@@ -686,7 +691,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     FastWarpSmem* ws = reinterpret_cast<FastWarpSmem*>(smem_raw) + wib;
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw + kFastWarps * sizeof(FastWarpSmem)) +
-                     (size_t)wib * 2 * a.cap;
+                     (size_t)wib * (a.cap + a.cap_sorted);
     uint64_t* sorted = keys + a.cap;
     const uint32_t k = a.k;
     for (;;) {
@@ -749,15 +754,16 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                              });
             __syncwarp();
             const bool short_knn = a.mode == MODE_KNN && count < k;  // rounding corner: never expected
-            if (count > a.cap || short_knn) {
+            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
+            const bool ok = count <= a.cap && !short_knn &&
+                            (n_sel == 0 || select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted));
+            if (!ok) {
                 if (lane == 0) {
                     const uint32_t slot = atomicAdd(a.ovf_count, 1u);
                     a.ovf_list[slot] = (uint32_t)qi;
                 }
                 continue;
             }
-            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
-            if (n_sel > 0) select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap);
             emit_row<float>(a.mode, k, n_sel, count, row_base + qp.idx, a.out_idx, a.out_d2, a.out_found,
                             a.fill_last, a.r2,
                             [&](uint32_t j) {
@@ -929,10 +935,15 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
                 uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
+    // candidate buffer: 256 keys for kNN, 512 for radius (or 4k); selected
+    // prefix: k plus the few keys that share the k-th key's histogram bin
     uint32_t cap = 1;
     const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? 256 : 512, 4ull * k);
     while (cap < want) cap <<= 1;
-    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + 2 * (size_t)cap * sizeof(uint64_t)));
+    uint32_t cap_sorted = 1;
+    while (cap_sorted < k + k / 2 + 16) cap_sorted <<= 1;
+    cap_sorted = std::min(cap_sorted, cap);
+    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap + cap_sorted) * sizeof(uint64_t)));
     auto kern = ct.n ? fast_search_kernel<true> : fast_search_kernel<false>;
     if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
@@ -950,6 +961,7 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     a.k = k;
     a.r2 = radius * radius;  // sq_search_radius in real_t, nn_search.hpp:98
     a.cap = cap;
+    a.cap_sorted = cap_sorted;
     a.work = words;
     a.ovf_count = words + 1;
     a.ovf_list = words + 8;
