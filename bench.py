@@ -391,7 +391,7 @@ def run_reference(args, rank, world):
 
 
 def run_batch(args):
-    """configs[3]: 256 clouds, sizes log-uniform in [2,000, 200,000] (seed 3),
+    """The multi-cloud batch: 256 clouds, sizes log-uniform in [2,000, 200,000] (seed 3),
     each the outdoor-scene generator scaled to a cube side U(5, 50) m; knn k=32
     plus compute_features. Plain: one knn_search + one compute_features call per
     cloud. Batched: the whole batch as one CUDA-graph replay."""
@@ -457,7 +457,7 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """configs[4]: Poisson arrivals (rate 200/s for 60 s, seed 4); each request a
+    """The serving stream: Poisson arrivals (rate 200/s for 60 s, seed 4); each request a
     cloud of log-uniform size in [1,000, 500,000] points from the outdoor-scene
     generator (scaled to a cube side U(5, 50) m), k in {16, 32, 64},
     compute_features_selected([Verticality, Curvature, Planarity, Normal_z])
@@ -500,8 +500,8 @@ def run_serve(args):
 
 
 def run_optimal(args):
-    """configs[2]: the 4,000,000-point outdoor scene (seed 2), radius_search
-    r = 0.5 m, max_knn = 64 -> CSR on the device (mask -1) ->
+    """The 4,000,000-point outdoor scene (seed 2), radius search r = 0.5 m,
+    max_knn = 64 -> CSR on the device (radius_search_csr) ->
     compute_features_optimal(k_min=1, k_step=1, k_min_search=10). Per-feature
     errors against the FP64 oracle are measured by tests/test_gpu_accuracy.py."""
     import torch
@@ -514,11 +514,7 @@ def run_optimal(args):
     t = torch.from_numpy(outdoor_scene(n, seed=2)).cuda()
 
     def step():
-        idx, _ = pgeof.radius_search(t, t, 0.5, 64)
-        mask = idx >= 0
-        ptr = torch.zeros(n + 1, dtype=torch.int32, device="cuda")
-        ptr[1:] = torch.cumsum(mask.sum(1, dtype=torch.int32), 0, dtype=torch.int32)
-        nn = idx[mask]
+        nn, ptr = pgeof.radius_search_csr(t, t, 0.5, 64)  # padded table -> CSR on the device
         return pgeof.compute_features_optimal(t, nn, ptr, 1, 1, 10, check=False)
 
     for _ in range(max(args.warmup, 3)):

@@ -126,6 +126,17 @@ int pgeof_radius_search_f32(const float* data, int64_t n_data, const float* quer
                             float search_radius, uint32_t max_knn, int32_t* indices, float* sqr_dist,
                             pgeof_stream_t stream);
 
+/* Radius search straight to CSR neighbourhoods (no reference counterpart: pgeof
+ * builds this pair on the host from radius_search's padded table, README.md:
+ * 157-163). nn_ptr (n_query + 1 entries) and nn (capacity n_query * max_knn)
+ * receive, for every query, the indices radius_search would return in its row
+ * (nearest first, at most max_knn, the -1 padding dropped); nn_ptr[n_query] is
+ * the number of entries written. Requires n_query * max_knn < 2^32. Device
+ * pointers, asynchronous on `stream`. */
+int pgeof_radius_search_csr_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                                float search_radius, uint32_t max_knn, uint32_t* nn, uint32_t* nn_ptr,
+                                pgeof_stream_t stream);
+
 /* compute_geometric_features<float, 11>, include/pgeof.hpp:75-117.
  * features: (n_points, 11); rows with fewer than k_min neighbours are 0.
  * Errors: k_min < 1. */

@@ -40,6 +40,7 @@ __all__ = [
     "compute_features_optimal",
     "knn_search",
     "radius_search",
+    "radius_search_csr",
     "compute_features_selected",
     "set_eig_order",
     "get_eig_order",
@@ -216,6 +217,44 @@ def radius_search(data, query, search_radius, max_knn):
                                     float(search_radius), int(max_knn), idx.data_ptr(), d2.data_ptr(), s)
         return idx, d2
     return _ext.radius_search(data, query, search_radius, max_knn)
+
+
+def radius_search_csr(data, query, search_radius, max_knn):
+    """Radius search straight to the CSR pair that compute_features* take.
+
+    Returns (nn, nn_ptr), both uint32: row i's neighbours are
+    nn[nn_ptr[i]:nn_ptr[i + 1]], the non-padding entries of radius_search's row
+    i in the same order -- what pgeof's README builds on the host from the
+    padded table (README.md:157-163), done on the GPU. torch CUDA tensors stay
+    on the device; numpy arrays go through it and come back as numpy.
+    """
+    import torch
+
+    numpy_in = not _is_torch(data)
+    if numpy_in:
+        import numpy as np
+
+        if not (isinstance(data, np.ndarray) and data.dtype == np.float32 and isinstance(query, np.ndarray)
+                and query.dtype == np.float32):
+            raise TypeError("radius_search_csr expects float32 numpy arrays or float32 CUDA tensors")
+        data_t = torch.from_numpy(np.ascontiguousarray(data)).cuda()
+        query_t = data_t if query is data else torch.from_numpy(np.ascontiguousarray(query)).cuda()
+    else:
+        data_t, query_t = data, query
+    _dev_cloud(data_t, "data")
+    _dev_cloud(query_t, "query")
+    m, k = int(query_t.shape[0]), int(max_knn)
+    with torch.cuda.device(data_t.device):
+        s = int(torch.cuda.current_stream().cuda_stream)
+        nn = _uint32_empty(torch, max(m * k, 1), data_t.device)
+        nn_ptr = _uint32_empty(torch, m + 1, data_t.device)
+        _ext._dev_radius_search_csr(data_t.data_ptr(), data_t.shape[0], query_t.data_ptr(), m,
+                                    float(search_radius), k, nn.data_ptr(), nn_ptr.data_ptr(), s)
+        nnz = int(nn_ptr[m:].view(torch.int32).item())
+    nn = nn[:nnz]
+    if numpy_in:
+        return nn.view(torch.int32).cpu().numpy().view("uint32"), nn_ptr.view(torch.int32).cpu().numpy().view("uint32")
+    return nn, nn_ptr
 
 
 def compute_features_selected(xyz, search_radius, max_knn, selected_features):

@@ -184,7 +184,8 @@ int knn_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_
 }
 
 int radius_impl(const float* data, uint64_t n_data, const float* query, uint64_t n_query, float radius,
-                uint32_t max_knn, int32_t* indices, float* sqr_dist, bool query_is_data, cudaStream_t s) {
+                uint32_t max_knn, int32_t* indices, float* sqr_dist, bool query_is_data, cudaStream_t s,
+                uint32_t* found = nullptr) {
     if (n_query == 0 || max_knn == 0) return PGEOF_OK;
     GridIndex<float> grid;
     const float r = std::fabs(radius);
@@ -200,6 +201,7 @@ int radius_impl(const float* data, uint64_t n_data, const float* query, uint64_t
     out.indices = indices;
     out.sqr_dist = sqr_dist;
     out.radius_fill_last = true;
+    out.found = found;
     return launch_search<float>(grid, q, qstart, n_query, MODE_RADIUS, max_knn, radius, out, s);
 }
 
@@ -545,6 +547,34 @@ int pgeof_radius_search_f32(const float* data, int64_t n_data, const float* quer
         return fail(PGEOF_ERR_INVALID_ARGUMENT, "max knn size is greater than the data point cloud size");
     return radius_impl(data, n_data, query, n_query, search_radius, max_knn, indices, sqr_dist,
                        data == query && n_data == n_query, (cudaStream_t)stream);
+}
+
+int pgeof_radius_search_csr_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
+                                float search_radius, uint32_t max_knn, uint32_t* nn, uint32_t* nn_ptr,
+                                pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n_data, "data"));
+    PGEOF_TRY(check_cloud(n_query, "query"));
+    if ((int64_t)max_knn > n_data)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "max knn size is greater than the data point cloud size");
+    if ((uint64_t)n_query * max_knn >= 0xffffffffull)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "n_query * max_knn must stay below 2^32 for uint32 nn_ptr");
+    if (!nn_ptr || (!nn && n_query > 0 && max_knn > 0))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "nn and nn_ptr must not be NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t m = (uint64_t)n_query;
+    if (m == 0 || max_knn == 0) {
+        PGEOF_CUDA_TRY(cudaMemsetAsync(nn_ptr, 0, (m + 1) * sizeof(uint32_t), s));
+        return PGEOF_OK;
+    }
+    Scratch table, found, counts, partials;
+    PGEOF_TRY(table.alloc(m * max_knn * sizeof(int32_t), s));
+    PGEOF_TRY(found.alloc(m * sizeof(uint32_t), s));
+    PGEOF_TRY(counts.alloc(m * sizeof(uint32_t), s));
+    PGEOF_TRY(partials.alloc((m / 1024 + 1) * sizeof(uint32_t), s));
+    PGEOF_TRY(radius_impl(data, n_data, query, n_query, search_radius, max_knn, table.as<int32_t>(), nullptr,
+                          data == query && n_data == n_query, s, found.as<uint32_t>()));
+    return launch_csr_from_table(table.as<int32_t>(), found.as<uint32_t>(), m, max_knn, counts.as<uint32_t>(),
+                                 partials.as<uint32_t>(), nn_ptr, nn, s);
 }
 
 int pgeof_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,

@@ -113,6 +113,16 @@ int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const 
                         uint32_t k, uint32_t* indices, float* sqr_dist, uint32_t* work, uint32_t* ovf,
                         cudaStream_t s);
 
+// Exclusive scan of G counts into out[0..G] (out[G] = total) with caller-owned
+// partials (ceil(G / 1024) words).
+int exclusive_scan_into(const uint32_t* in, uint32_t G, uint32_t* out, uint32_t* partials, cudaStream_t s);
+
+// Radius-search table (m, max_knn) + uncapped counts -> CSR: nn_ptr[0..m] and
+// the first min(found, max_knn) entries of each row packed into nn. `counts`
+// (m words) and `partials` (ceil(m / 1024) words) are scratch.
+int launch_csr_from_table(const int32_t* table, const uint32_t* found, uint64_t m, uint32_t max_knn,
+                          uint32_t* counts, uint32_t* partials, uint32_t* nn_ptr, uint32_t* nn, cudaStream_t s);
+
 // PCA + selected features from a radius-search neighbour table (selected path).
 template <typename T>
 int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint32_t* found, uint32_t max_knn,

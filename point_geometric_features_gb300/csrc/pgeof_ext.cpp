@@ -310,6 +310,12 @@ PYBIND11_MODULE(pgeof_ext, m) {
         check(pgeof_radius_search_f32(P<const float>(data), n, P<const float>(query), m_, r, k, P<int32_t>(idx),
                                       P<float>(d2), P<void>(stream)));
     });
+    m.def("_dev_radius_search_csr", [](uintptr_t data, int64_t n, uintptr_t query, int64_t m_, float r, uint32_t k,
+                                       uintptr_t nn, uintptr_t nn_ptr, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_radius_search_csr_f32(P<const float>(data), n, P<const float>(query), m_, r, k, P<uint32_t>(nn),
+                                          P<uint32_t>(nn_ptr), P<void>(stream)));
+    });
     m.def("_dev_compute_features", [](uintptr_t xyz, int64_t n_xyz, uintptr_t nn, int64_t nnz, uintptr_t ptr,
                                       int64_t n, uint64_t k_min, uintptr_t out, uintptr_t stream) {
         py::gil_scoped_release nogil;

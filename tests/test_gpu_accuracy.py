@@ -1,4 +1,4 @@
-"""configs[2]: the 4M-point outdoor scene, radius_search(r=0.5, max_knn=64) ->
+"""The 4M-point outdoor scene (seed 2), radius_search(r=0.5, max_knn=64) ->
 CSR -> compute_features_optimal(k_min=1, k_step=1, k_min_search=10), with each
 feature's error against the FP64 oracle (numpy float64 restatement of
 include/pca.hpp / include/pgeof.hpp:243-310) on a 3,000-row sample.
@@ -6,7 +6,7 @@ include/pca.hpp / include/pgeof.hpp:243-310) on a 3,000-row sample.
 Reported per feature: max |gpu - fp64| and max relative error (|x| > 1e-3),
 the normal's angle error (radians, sign-agnostic), the agreement of the
 optimal k with the FP32-literal oracle and with the FP64 argmin. Bounds: the
-the benchmark spec's 1e-4 abs on linearity / planarity / scattering / verticality and
+1e-4 abs target on linearity / planarity / scattering / verticality and
 1e-3 rad on normals hold for the rows whose eigenvectors are well conditioned
 (relative eigen-gap >= 1e-3); the ascending-order Scattering reaches ~1e3, so
 the 1e-4 bound is applied relative to max(1, |x|).
@@ -35,7 +35,7 @@ def _fp64_optimal(P, k0, k_nn):
     return best_k
 
 
-def test_c3_optimal_4m_errors_vs_fp64(cuda, pgeof):
+def test_optimal_4m_errors_vs_fp64(cuda, pgeof):
     torch = cuda
     xyz = outdoor_scene(4_000_000, seed=2)
     t = torch.from_numpy(xyz).cuda()

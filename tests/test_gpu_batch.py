@@ -1,4 +1,4 @@
-"""Multi-cloud batches (configs[3] shape, scaled down): one device pipeline
+"""Multi-cloud batches (the 256-cloud workload's shape, scaled down): one device pipeline
 over many clouds of uneven size must equal per-cloud knn_search +
 compute_features calls exactly, also when replayed from a CUDA graph on new
 data."""

@@ -48,7 +48,7 @@ def test_golden_features(cuda, pgeof, golden):
 
 
 def test_c1_uniform_10k_k20(cuda, pgeof):
-    """configs[0]: 10k uniform points, knn k=20 -> CSR -> compute_features(k_min=1)."""
+    """10k uniform points, knn k=20 -> CSR -> compute_features(k_min=1)."""
     xyz = uniform_cube(10_000, seed=0)
     idx, _ = pgeof.knn_search(xyz, xyz, 20)
     nn, nn_ptr = _csr(idx)
@@ -64,7 +64,7 @@ def test_c1_uniform_10k_k20(cuda, pgeof):
 
 
 def test_scene_multiscale(cuda, pgeof):
-    """configs[1] shape at 50k points: knn k=50 -> multiscale [10, 20, 50]."""
+    """The outdoor scene at 50k points: knn k=50 -> multiscale [10, 20, 50]."""
     xyz = outdoor_scene(50_000, seed=1)
     idx, _ = pgeof.knn_search(xyz, xyz, 50)
     nn, nn_ptr = _csr(idx)
@@ -103,7 +103,7 @@ def test_many_scales(cuda, pgeof):
 
 
 def test_optimal_radius_csr(cuda, pgeof):
-    """configs[2] shape at 40k points: radius 0.5 / max 64 -> optimal(k_min=1, k_step=1, k_min_search=10)."""
+    """The outdoor scene at 40k points: radius 0.5 / max 64 -> optimal(k_min=1, k_step=1, k_min_search=10)."""
     xyz = outdoor_scene(40_000, seed=2)
     idx, _ = pgeof.radius_search(xyz, xyz, 0.5, 64)
     nn, nn_ptr = _radius_csr(idx)

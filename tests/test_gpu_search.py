@@ -167,3 +167,52 @@ def test_knn_deterministic(cuda, pgeof):
     b = pgeof.knn_search(xyz, xyz, 32)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def _csr_from_table(idx):
+    """pgeof README.md:157-163: drop the -1 padding, row counts -> offsets."""
+    idx = np.asarray(idx)
+    mask = idx >= 0
+    ptr = np.zeros(idx.shape[0] + 1, np.uint32)
+    ptr[1:] = np.cumsum(mask.sum(1))
+    return idx[mask].astype(np.uint32), ptr
+
+
+@pytest.mark.parametrize("max_knn", [1, 7, 64])
+def test_radius_search_csr_matches_padded_table(cuda, pgeof, max_knn):
+    torch = cuda
+    xyz = outdoor_scene(60_000, seed=13)
+    t = torch.from_numpy(xyz).cuda()
+    for q, r in ((t, 0.5), (torch.from_numpy(uniform_cube(5_000, seed=3, side=100.0)).cuda(), 2.0)):
+        idx, _ = pgeof.radius_search(t, q, r, max_knn)
+        nn, ptr = pgeof.radius_search_csr(t, q, r, max_knn)
+        ref_nn, ref_ptr = _csr_from_table(idx.cpu().numpy())
+        np.testing.assert_array_equal(ptr.view(torch.int32).cpu().numpy().view(np.uint32), ref_ptr)
+        np.testing.assert_array_equal(nn.view(torch.int32).cpu().numpy().view(np.uint32), ref_nn)
+    # numpy in, numpy out; against the oracle's own table on a small case
+    small = xyz[:3_000]
+    nn, ptr = pgeof.radius_search_csr(small, small, 0.7, 16)
+    o_idx, _ = oracle.radius_search(small, small, 0.7, 16)
+    ref_nn, ref_ptr = _csr_from_table(o_idx)
+    assert nn.dtype == np.uint32 and ptr.dtype == np.uint32
+    np.testing.assert_array_equal(ptr, ref_ptr)
+    np.testing.assert_array_equal(nn, ref_nn)
+
+
+def test_radius_search_csr_edges(cuda, pgeof):
+    torch = cuda
+    xyz = torch.from_numpy(uniform_cube(1_000, seed=2)).cuda()
+    far = xyz + 1000.0  # no neighbour within the radius for any query
+    nn, ptr = pgeof.radius_search_csr(xyz, far, 0.1, 8)
+    assert nn.numel() == 0 and int(ptr.view(torch.int32).max()) == 0 and ptr.numel() == 1_001
+    nn, ptr = pgeof.radius_search_csr(xyz, xyz[:0], 0.1, 8)
+    assert nn.numel() == 0 and ptr.numel() == 1
+    with pytest.raises(ValueError):
+        pgeof.radius_search_csr(xyz, xyz, 0.1, 2_000)  # max_knn > n
+    # the CSR feeds compute_features_optimal directly
+    nn, ptr = pgeof.radius_search_csr(xyz, xyz, 0.3, 32)
+    out = pgeof.compute_features_optimal(xyz, nn, ptr, 1, 1, 5)
+    idx, _ = pgeof.radius_search(xyz, xyz, 0.3, 32)
+    ref_nn, ref_ptr = _csr_from_table(idx.cpu().numpy())
+    ref = pgeof.compute_features_optimal(xyz.cpu().numpy(), ref_nn, ref_ptr, 1, 1, 5)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)

@@ -28,7 +28,7 @@ def test_golden_selected(cuda, pgeof, golden):
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_selected_scene(cuda, pgeof, dtype):
-    """configs[4]'s feature list [Verticality, Curvature, Planarity, Normal_z]."""
+    """The serving workload's feature list [Verticality, Curvature, Planarity, Normal_z]."""
     xyz = outdoor_scene(20_000, seed=5).astype(dtype)
     ids = [pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z]
     out = pgeof.compute_features_selected(xyz, 0.4, 32, ids)

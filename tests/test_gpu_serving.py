@@ -1,4 +1,4 @@
-"""Serving (configs[4] shape, scaled down): requests admitted while others run
+"""Serving (the Poisson request stream, scaled down): requests admitted while others run
 overlap on the GPU, and every result equals the same request run alone."""
 
 import numpy as np
