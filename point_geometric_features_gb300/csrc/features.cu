@@ -55,13 +55,37 @@ struct RowCloud {
     uint32_t n;
 };
 
-__device__ __forceinline__ float4 load_nb(const FeatArgs& a, const RowCloud& rc, uint64_t pos, uint32_t& flags) {
-    uint32_t id = __ldg(a.nn + pos);
+__device__ __forceinline__ float4 gather_nb(const RowCloud& rc, uint32_t id, uint32_t& flags) {
     if (id >= rc.n) {
         flags |= ERR_NN_RANGE;
         id = 0;
     }
     return __ldg(rc.xyz4 + id);
+}
+
+// Calls f(j, point) for the row's neighbours j = 0 .. kmax-1 in order. Indices
+// are read four at a time (16-byte loads once the row pointer is aligned),
+// which quarters the L1 requests for them, and each group's four gathers are
+// issued before any is used.
+template <typename F>
+__device__ __forceinline__ void for_each_nb(const FeatArgs& a, const RowCloud& rc, uint64_t b, uint32_t kmax,
+                                            uint32_t& flags, F&& f) {
+    const uint32_t* nn = a.nn + b;
+    uint32_t j = 0;
+    while (j < kmax && (reinterpret_cast<uintptr_t>(nn + j) & 15u)) {
+        f(j, gather_nb(rc, __ldg(nn + j), flags));
+        ++j;
+    }
+    for (; j + 4 <= kmax; j += 4) {
+        const uint4 ids = __ldg(reinterpret_cast<const uint4*>(nn + j));
+        const float4 p0 = gather_nb(rc, ids.x, flags), p1 = gather_nb(rc, ids.y, flags);
+        const float4 p2 = gather_nb(rc, ids.z, flags), p3 = gather_nb(rc, ids.w, flags);
+        f(j, p0);
+        f(j + 1, p1);
+        f(j + 2, p2);
+        f(j + 3, p3);
+    }
+    for (; j < kmax; ++j) f(j, gather_nb(rc, __ldg(nn + j), flags));
 }
 
 template <int S, bool MULTI>
@@ -118,8 +142,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             float mx[S], my[S], mz[S];
 #pragma unroll
             for (int s = 0; s < S; ++s) mx[s] = my[s] = mz[s] = 0.0f;
-            for (uint32_t j = 0; j < kmax; ++j) {
-                const float4 p = load_nb(a, rc, (uint64_t)b + j, flags);
+            for_each_nb(a, rc, b, kmax, flags, [&](uint32_t j, const float4& p) {
                 rx = FADD(rx, p.x);
                 ry = FADD(ry, p.y);
                 rz = FADD(rz, p.z);
@@ -134,7 +157,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                         }
                     }
                 }
-            }
+            });
             if constexpr (S == 1) {
                 const float kk = (float)ks[0];
                 mx[0] = FDIV(rx, kk);
@@ -145,8 +168,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             float cxx[S], cxy[S], cxz[S], cyy[S], cyz[S], czz[S];
 #pragma unroll
             for (int s = 0; s < S; ++s) cxx[s] = cxy[s] = cxz[s] = cyy[s] = cyz[s] = czz[s] = 0.0f;
-            for (uint32_t j = 0; j < kmax; ++j) {
-                const float4 p = load_nb(a, rc, (uint64_t)b + j, flags);
+            for_each_nb(a, rc, b, kmax, flags, [&](uint32_t j, const float4& p) {
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
                     if (s < n_active && j < ks[s]) {
@@ -161,7 +183,7 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                         czz[s] = FADD(czz[s], FMUL(dz, dz));
                     }
                 }
-            }
+            });
             if constexpr (S == 1) {
                 const float kk = (float)ks[0];
                 Cov<float> c;
