@@ -371,7 +371,7 @@ def run_reference(args, rank, world):
         "metric": METRIC,
         "value": round(value, 1),
         "unit": UNIT,
-        "n_gpus": 0,
+        "n_gpus": world,  # GPUs of the launch; the timed work runs on rank 0's host cores
         "steps": args.steps,
         "warmup": max(args.warmup, 1),
         "ms_per_step": round(N_POINTS / value * 1e3, 3),
