@@ -557,6 +557,8 @@ struct FastArgs {
     float r2;
     uint32_t cap;         // power of two, candidate keys per warp
     uint32_t cap_sorted;  // power of two, selected keys per warp
+    const uint32_t* qlist;   // LIST pass: positions in `queries` to process ...
+    const uint32_t* qcount;  // ... and their number (device)
     uint32_t* work;
     uint32_t* ovf_list;
     uint32_t* ovf_count;
@@ -685,7 +687,10 @@ __device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* 
     return true;
 }
 
-template <bool MULTI>
+// LIST: a second pass over the queries whose key buffer overflowed in the
+// first (a.qlist / a.qcount), each with its pilot bound -- the first pass's
+// bound came from a solved neighbour and was too loose -- and a larger buffer.
+template <bool MULTI, bool LIST>
 __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __grid_constant__ FastArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -694,17 +699,20 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                      (size_t)wib * (a.cap + a.cap_sorted);
     uint64_t* sorted = keys + a.cap;
     const uint32_t k = a.k;
+    const uint64_t m = LIST ? (uint64_t)*a.qcount : a.m;
+    constexpr int chunk_len = LIST ? 1 : kChunk;  // list queries are few and costly: one per work item
     for (;;) {
         uint32_t chunk = 0;
         if (lane == 0) chunk = atomicAdd(a.work, 1u);
         chunk = __shfl_sync(FULL, chunk, 0);
-        const uint64_t q0 = (uint64_t)chunk * kChunk;
-        if (q0 >= a.m) break;
-        const uint64_t q1 = min(q0 + (uint64_t)kChunk, a.m);
+        const uint64_t q0 = (uint64_t)chunk * chunk_len;
+        if (q0 >= m) break;
+        const uint64_t q1 = min(q0 + (uint64_t)chunk_len, m);
         // the last 32 solved queries of this chunk, one per lane: position and d_k
         float rx = 0.0f, ry = 0.0f, rz = 0.0f, rdk = -1.0f;
         int rci = -1;
-        for (uint64_t qi = q0; qi < q1; ++qi) {
+        for (uint64_t qpos = q0; qpos < q1; ++qpos) {
+            const uint64_t qi = LIST ? (uint64_t)a.qlist[qpos] : qpos;
             const SPoint<float> qp = a.queries[qi];
             GridView<float> gv = a.gv;
             uint64_t row_base = 0;
@@ -723,7 +731,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                 strict = false;
                 // d_k(q) <= d_k(p) + |q - p| for every solved p: take the best over the lanes
                 float bound = INFINITY;
-                if (rdk >= 0.0f && rci == ci) {
+                if (!LIST && rdk >= 0.0f && rci == ci) {
                     const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
                     const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
                     if (dq <= 0.75f * rdk) bound = rdk + dq;
@@ -773,7 +781,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                                 e.idx = (uint32_t)key;
                                 return e;
                             });
-            if (a.mode == MODE_KNN && lane == (int)(qi & 31)) {
+            if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
                 rdk = sqrtf(key_d2(sorted[k - 1]));
                 rx = q[0];
                 ry = q[1];
@@ -931,8 +939,12 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
 
 // The fast kernel over `queries` (cell order), then the general kernel over the
 // queries whose buffer overflowed. `words`: 8 zeroed words + m words.
+// `words`: 8 + m words of scratch (work counter, overflow count, overflow
+// list). With `words2` (another 8 + m words) the overflowing queries get a
+// second fast pass (pilot bounds, a 1024-key buffer) before the general kernel.
 int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<float>* queries, uint64_t m, int mode,
-                uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, cudaStream_t s) {
+                uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, uint32_t* words2,
+                cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     // candidate buffer: 256 keys for kNN, 512 for radius (or 4k); selected
@@ -944,7 +956,7 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     while (cap_sorted < k + k / 2 + 16) cap_sorted <<= 1;
     cap_sorted = std::min(cap_sorted, cap);
     const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap + cap_sorted) * sizeof(uint64_t)));
-    auto kern = ct.n ? fast_search_kernel<true> : fast_search_kernel<false>;
+    auto kern = ct.n ? fast_search_kernel<true, false> : fast_search_kernel<false, false>;
     if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
     PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastWarps * 32, smem));
@@ -976,6 +988,34 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     }
     count_launch();
     PGEOF_TRY(check_launch("fast_search_kernel"));
+    if (words2 && !ct.n) {
+        // second pass over the overflow list, sized on the device
+        uint32_t cap2 = 1;
+        while (cap2 < std::max<uint64_t>(1024, 4ull * k)) cap2 <<= 1;
+        const int smem2 =
+            (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t)));
+        auto kern2 = fast_search_kernel<false, true>;
+        if (smem2 > 48 * 1024)
+            PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        int per_sm2 = 0;
+        PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, kern2, kFastWarps * 32, smem2));
+        per_sm2 = std::max(per_sm2, 1);
+        PGEOF_CUDA_TRY(cudaMemsetAsync(words2, 0, 8 * sizeof(uint32_t), s));
+        FastArgs a2 = a;
+        a2.cap = cap2;
+        a2.qlist = a.ovf_list;
+        a2.qcount = a.ovf_count;
+        a2.work = words2;
+        a2.ovf_count = words2 + 1;
+        a2.ovf_list = words2 + 8;
+        {
+            KernelTimer kt("overflow_search_kernel", s);
+            kern2<<<(unsigned)((uint64_t)di->sm_count * per_sm2), kFastWarps * 32, smem2, s>>>(a2);
+        }
+        count_launch();
+        PGEOF_TRY(check_launch("fast_search_kernel(list)"));
+        return launch_general_view<float>(gv, ct, queries, m, a2.ovf_list, a2.ovf_count, mode, k, radius, out, s);
+    }
     // queries whose key buffer overflowed: the general kernel, sized on the device
     return launch_general_view<float>(gv, ct, queries, m, a.ovf_list, a.ovf_count, mode, k, radius, out, s);
 }
@@ -993,12 +1033,13 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
         if (k > 128 || m >= 0xffffffffull)
             return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
         Scratch ctl;
-        PGEOF_TRY(ctl.alloc((m + 8) * sizeof(uint32_t), s));
+        PGEOF_TRY(ctl.alloc(2 * (m + 8) * sizeof(uint32_t), s));
         GridView<float> gv;
         gv.g = grid.g;
         gv.cell_start = grid.cell_start;
         gv.pts = grid.pts;
-        return launch_fast(gv, CloudTable{}, queries, m, mode, k, radius, out, ctl.as<uint32_t>(), s);
+        return launch_fast(gv, CloudTable{}, queries, m, mode, k, radius, out, ctl.as<uint32_t>(),
+                           ctl.as<uint32_t>() + m + 8, s);
     }
 }
 
@@ -1015,7 +1056,7 @@ int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const 
     if (k > 128)
         return launch_general_view<float>(gv, ct, pts, n_points, nullptr, nullptr, MODE_KNN, k, 0.0f, out, s);
     (void)ovf;
-    return launch_fast(gv, ct, pts, n_points, MODE_KNN, k, 0.0f, out, work, s);
+    return launch_fast(gv, ct, pts, n_points, MODE_KNN, k, 0.0f, out, work, nullptr, s);
 }
 
 template <typename T>
