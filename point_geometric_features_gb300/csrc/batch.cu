@@ -55,13 +55,8 @@ __global__ void batch_bbox_kernel(const float* __restrict__ xyz, const uint64_t*
             mx[a] = fmaxf(mx[a], v);
         }
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-        }
-    if ((threadIdx.x & 31) == 0 && e > b) {
+    block_box_reduce(mn, mx);
+    if (threadIdx.x == 0 && e > b) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             atomicMin(box + 6 * c + a, ord_key(mn[a]));

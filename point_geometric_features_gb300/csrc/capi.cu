@@ -342,6 +342,14 @@ int host_selected(const T* xyz, int64_t n, T radius, uint32_t max_knn, const int
     return finish_host(ce, s);
 }
 
+struct OccEntry {
+    int device;
+    const void* kernel;
+    int threads, smem, per_sm;
+};
+std::mutex g_occ_mu;
+std::vector<OccEntry> g_occ;
+
 // Cache of page-locked host blocks behind pgeof_host_alloc / pgeof_host_free.
 struct HostPool {
     std::mutex mu;
@@ -365,6 +373,28 @@ size_t host_pool_cap(HostPool& hp) {
 }
 
 }  // namespace
+
+int pgeof::kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* per_sm) {
+    int dev = 0;
+    PGEOF_CUDA_TRY(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> lk(g_occ_mu);
+        for (const OccEntry& e : g_occ)
+            if (e.device == dev && e.kernel == kernel && e.threads == threads && e.smem == smem) {
+                *per_sm = e.per_sm;
+                return PGEOF_OK;
+            }
+    }
+    if (smem > 48 * 1024)
+        PGEOF_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int n = 0;
+    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem));
+    n = std::max(n, 1);
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    g_occ.push_back(OccEntry{dev, kernel, threads, smem, n});
+    *per_sm = n;
+    return PGEOF_OK;
+}
 
 // =========================================================================
 extern "C" {

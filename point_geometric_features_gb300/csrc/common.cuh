@@ -70,6 +70,12 @@ struct DeviceInfo {
 };
 int current_device_info(const DeviceInfo** out);
 
+// Resident blocks per SM of `kernel` at `threads` threads and `smem` bytes of
+// dynamic shared memory on the current device, raising the kernel's shared
+// memory limit first when smem > 48 KB. Cached per (device, kernel, threads,
+// smem), so repeated launches pay no host-side query.
+int kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* per_sm);
+
 // ----------------------------------------------------------------- scratch
 // Stream-ordered scratch allocations from a library-owned memory pool that
 // keeps freed blocks cached (no OS round trip per call).

@@ -46,14 +46,8 @@ __global__ void bbox_kernel(const T* __restrict__ xyz, uint64_t n, uint32_t* out
             mx[a] = fmaxf(mx[a], v);
         }
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        for (int o = 16; o > 0; o >>= 1) {
-            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-        }
-    }
-    if ((threadIdx.x & 31) == 0) {
+    block_box_reduce(mn, mx);
+    if (threadIdx.x == 0) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             atomicMin(out6 + a, ord_key(mn[a]));

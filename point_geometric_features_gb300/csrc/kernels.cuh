@@ -30,6 +30,39 @@ struct GridParams {
     float margin;      // slack added to every cell-distance bound
 };
 
+// Min / max of three coordinates over the block (blockDim.x a multiple of 32,
+// every thread calls it); thread 0 holds the result. One atomic per value and
+// block then replaces one per warp, which serialised on six addresses.
+__device__ __forceinline__ void block_box_reduce(float (&mn)[3], float (&mx)[3]) {
+    __shared__ float part[6][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            part[a][w] = mn[a];
+            part[3 + a][w] = mx[a];
+        }
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = lane < nw ? part[a][lane] : INFINITY;
+            mx[a] = lane < nw ? part[3 + a][lane] : -INFINITY;
+            for (int o = 16; o > 0; o >>= 1) {
+                mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+                mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+            }
+        }
+    }
+}
+
 // A point in cell order: coordinates plus its original row index.
 template <typename T>
 struct SPoint;

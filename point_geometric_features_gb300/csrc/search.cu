@@ -892,10 +892,8 @@ int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoin
     const bool in_smem = general_smem_bytes<T>(cap, true) <= std::min(di->max_smem_optin, 200 * 1024);
     const int smem = general_smem_bytes<T>(cap, in_smem);
     auto kern = search_kernel<T>;
-    if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
-    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSearchWarps * 32, smem));
-    per_sm = std::max(per_sm, 1);
+    PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kSearchWarps * 32, smem, &per_sm));
     const uint64_t blocks = std::min<uint64_t>(ceil_div_u(m, kSearchWarps), (uint64_t)di->sm_count * per_sm);
     Scratch gbuf;
     SearchArgs<T> a{};
@@ -957,10 +955,8 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     cap_sorted = std::min(cap_sorted, cap);
     const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap + cap_sorted) * sizeof(uint64_t)));
     auto kern = ct.n ? fast_search_kernel<true, false> : fast_search_kernel<false, false>;
-    if (smem > 48 * 1024) PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
-    PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFastWarps * 32, smem));
-    per_sm = std::max(per_sm, 1);
+    PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kFastWarps * 32, smem, &per_sm));
     const uint64_t chunks = ceil_div_u(m, kChunk);
     const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
     PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
@@ -995,11 +991,8 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
         const int smem2 =
             (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t)));
         auto kern2 = fast_search_kernel<false, true>;
-        if (smem2 > 48 * 1024)
-            PGEOF_CUDA_TRY(cudaFuncSetAttribute(kern2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
         int per_sm2 = 0;
-        PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, kern2, kFastWarps * 32, smem2));
-        per_sm2 = std::max(per_sm2, 1);
+        PGEOF_TRY(kernel_blocks_per_sm((const void*)kern2, kFastWarps * 32, smem2, &per_sm2));
         PGEOF_CUDA_TRY(cudaMemsetAsync(words2, 0, 8 * sizeof(uint32_t), s));
         FastArgs a2 = a;
         a2.cap = cap2;
