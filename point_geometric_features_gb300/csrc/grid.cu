@@ -342,7 +342,12 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
     for (int a = 0; a < 3; ++a) ext_max = std::max(ext_max, (double)b.mx[a] - (double)b.mn[a]);
     double vol = 1.0;
     for (int a = 0; a < 3; ++a) vol *= std::max((double)b.mx[a] - (double)b.mn[a], ext_max * 1e-3);
-    const double target = std::min(48.0, std::max(2.0, (double)k_target / 3.5));
+    // Occupancy target (points per cell, point-weighted): k / 3.5 for clouds of
+    // surfaces, finer cells for volume-filling clouds -- on a uniform cube
+    // k / 12 is 19% faster at k = 50 than k / 3.5, on an outdoor scene of
+    // walls and ground k / 3.5 is best. The dimension comes from two trial
+    // histograms: (occupancy - 1) scales as h^dim (the 1 is the point itself).
+    const double target2 = std::min(48.0, std::max(2.0, (double)k_target / 3.5));
     const uint64_t cap = std::max<uint64_t>(4 * n, 1u << 16);
     const double hmin = h_min > 0 ? (double)h_min : 0.0;
     const double hmax = h_max > 0 ? (double)h_max : 1e300;
@@ -354,7 +359,7 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
         while (!make_params(b, h, cap, g)) h *= 1.25;
         return h;
     };
-    double h0 = clamp_h(std::cbrt(vol * target / (double)n));
+    double h0 = clamp_h(std::cbrt(vol * target2 / (double)n));
     double h = h0;
     EdgeKey key{n, k_target, h_min, h_max, {b.mn[0], b.mn[1], b.mn[2], b.mx[0], b.mx[1], b.mx[2]}};
     double cached = 0.0;
@@ -365,23 +370,43 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
         make_params(b, h0, cap, g);
         Scratch cnt;
         PGEOF_TRY(cnt.alloc((size_t)cap * sizeof(uint32_t), s));
+        unsigned long long* acc = reinterpret_cast<unsigned long long*>(box + 8);
         double m0 = 0.0;
-        PGEOF_TRY(occupancy<T>(xyz, n, g, cnt.as<uint32_t>(), reinterpret_cast<unsigned long long*>(box + 8), m0,
-                               s));
-        if (!(m0 > target / 1.6 && m0 < target * 1.6) && m0 > 0.0) {
-            double h1 = clamp_h(h0 * std::min(16.0, std::max(1.0 / 16.0, std::sqrt(target / m0))));
+        PGEOF_TRY(occupancy<T>(xyz, n, g, cnt.as<uint32_t>(), acc, m0, s));
+        // surfaces: move towards target2 until a trial lands within 60% of it
+        double h1 = h0, m1 = 0.0;
+        if (!(m0 > target2 / 1.6 && m0 < target2 * 1.6) && m0 > 0.0) {
+            h1 = clamp_h(h0 * std::min(16.0, std::max(1.0 / 16.0, std::sqrt(target2 / m0))));
             if (h1 != h0) {
                 make_params(b, h1, cap, g);
-                double m1 = 0.0;
-                PGEOF_TRY(occupancy<T>(xyz, n, g, cnt.as<uint32_t>(),
-                                       reinterpret_cast<unsigned long long*>(box + 8), m1, s));
+                PGEOF_TRY(occupancy<T>(xyz, n, g, cnt.as<uint32_t>(), acc, m1, s));
                 h = h1;
-                if (!(m1 > target / 1.6 && m1 < target * 1.6) && m1 > 0.0 && m0 != m1) {
+                if (!(m1 > target2 / 1.6 && m1 < target2 * 1.6) && m1 > 0.0 && m0 != m1) {
                     double dim = std::log(m0 / m1) / std::log(h0 / h1);
                     if (!std::isfinite(dim)) dim = 2.0;
                     dim = std::min(3.0, std::max(1.0, dim));
-                    h = clamp_h(h1 * std::pow(target / m1, 1.0 / dim));
+                    h = clamp_h(h1 * std::pow(target2 / m1, 1.0 / dim));
                 }
+            }
+        } else if (m0 > 0.0) {
+            // on target at the first trial: a half-edge trial for the dimension
+            h1 = clamp_h(h0 * 0.5);
+            if (h1 != h0) {
+                make_params(b, h1, cap, g);
+                PGEOF_TRY(occupancy<T>(xyz, n, g, cnt.as<uint32_t>(), acc, m1, s));
+            }
+        }
+        // volume-filling clouds: finer cells, placed by (m - 1) ~ h^dim
+        if (m0 > 1.05 && m1 > 1.05 && h1 != h0) {
+            double dim = std::log((m0 - 1.0) / (m1 - 1.0)) / std::log(h0 / h1);
+            if (!std::isfinite(dim)) dim = 2.0;
+            dim = std::min(3.0, std::max(1.0, dim));
+            const double w = std::min(1.0, std::max(0.0, (dim - 2.3) / 0.6));
+            if (w > 0.0) {
+                const double target = std::min(48.0, std::max(2.0, (double)k_target / (3.5 + 8.5 * w)));
+                const bool use1 = std::fabs(std::log(m1 / target)) < std::fabs(std::log(m0 / target));
+                const double hr = use1 ? h1 : h0, mr = use1 ? m1 : m0;
+                h = clamp_h(hr * std::pow((target - 1.0) / (mr - 1.0), 1.0 / dim));
             }
         }
     }
