@@ -226,6 +226,22 @@ def run_ours(args, rank, world, local):
     pgeof.check_device_errors()
     assert out.shape == (N_POINTS, len(SCALES), 11) and bool(torch.isfinite(out).all())
 
+    # the same kNN + multiscale features through the fused feature-only
+    # pipeline (neighbour lists stay on the device, no distances written)
+    for _ in range(2):
+        fused = pgeof.knn_features(t, K, SCALES)
+    torch.cuda.synchronize()
+    f_ms = 0.0
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record()
+        fused = pgeof.knn_features(t, K, SCALES)
+        stops[i].record()
+    torch.cuda.synchronize()
+    f_ms = sum(s.elapsed_time(e) for s, e in zip(starts, stops))
+    assert torch.equal(fused, out)
+    f_ms = max_over_ranks(f_ms, device=dev)
+
     # e2e: the numpy drop-in API, host buffers in and out
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
     nn_ptr_h = (np.arange(N_POINTS + 1, dtype=np.int64) * K).astype(np.uint32)
@@ -295,6 +311,9 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": round(world * N_POINTS * e2e_steps / e2e_s, 1) if e2e_steps else None, "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "numpy drop-in API (pageable host inputs, results in the library's cached page-locked blocks)", "steps": e2e_steps},
+        "fused": {"value": round(world * N_POINTS * args.steps / (f_ms / 1e3), 1), "unit": UNIT,
+                  "ms_per_step": round(f_ms / args.steps, 4),
+                  "path": "knn_features: one device pipeline, neighbour lists in cell order, no distances"},
         "gpu_launches": int(launches),
         "clocks": clk,
         "roofline": roofline,

@@ -152,6 +152,17 @@ int pgeof_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const
                                           const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
                                           int64_t n_scales, float* features, pgeof_stream_t stream);
 
+/* kNN + features in one device pipeline for feature-only callers (no
+ * reference counterpart: the reference composes knn_search and
+ * compute_features* through host arrays). Writes what
+ * compute_features(xyz, knn_search(xyz, xyz, knn)) writes when n_scales == 0
+ * (n x 11), or compute_features_multiscale(..., k_scales) (n x n_scales x 11)
+ * with k_scales ascending and <= knn. The neighbour lists stay in device
+ * scratch in cell order and no distances are written. Device pointers;
+ * k_scales is a host array. */
+int pgeof_knn_features_f32(const float* xyz, int64_t n, uint32_t knn, const uint32_t* k_scales, int64_t n_scales,
+                           float* features, pgeof_stream_t stream);
+
 /* compute_geometric_features_optimal<float, 12>, include/pgeof.hpp:243-310.
  * features: (n_points, 12); column 11 holds the optimal k as a float.
  * Errors: k_min < 1 and k_min_search < 1; k_step == 0 (the reference divides

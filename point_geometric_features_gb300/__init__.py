@@ -41,6 +41,7 @@ __all__ = [
     "knn_search",
     "radius_search",
     "radius_search_csr",
+    "knn_features",
     "compute_features_selected",
     "set_eig_order",
     "get_eig_order",
@@ -255,6 +256,38 @@ def radius_search_csr(data, query, search_radius, max_knn):
     if numpy_in:
         return nn.view(torch.int32).cpu().numpy().view("uint32"), nn_ptr.view(torch.int32).cpu().numpy().view("uint32")
     return nn, nn_ptr
+
+
+def knn_features(xyz, k, k_scales=None):
+    """kNN + local PCA features in one device pipeline, for callers that want
+    only the features.
+
+    Returns what compute_features(xyz, *knn_search(xyz, xyz, k) as CSR) returns
+    -- (n, 11) -- or, with k_scales (ascending, each <= k),
+    compute_features_multiscale over the same kNN lists -- (n, len(k_scales),
+    11). The neighbour lists never leave the GPU and no distances are written.
+    torch CUDA tensors stay on the device; numpy arrays go through it.
+    """
+    import torch
+
+    numpy_in = not _is_torch(xyz)
+    if numpy_in:
+        import numpy as np
+
+        if not (isinstance(xyz, np.ndarray) and xyz.dtype == np.float32):
+            raise TypeError("knn_features expects a float32 numpy array or a float32 CUDA tensor")
+        t = torch.from_numpy(np.ascontiguousarray(xyz)).cuda()
+    else:
+        t = xyz
+    _dev_cloud(t, "xyz")
+    scales = [int(v) for v in k_scales] if k_scales is not None else []
+    n = int(t.shape[0])
+    shape = (n, len(scales), 11) if scales else (n, 11)
+    with torch.cuda.device(t.device):
+        s = int(torch.cuda.current_stream().cuda_stream)
+        out = torch.zeros(shape, dtype=torch.float32, device=t.device)
+        _ext._dev_knn_features(t.data_ptr(), n, int(k), scales, out.data_ptr(), s)
+    return out.cpu().numpy() if numpy_in else out
 
 
 def compute_features_selected(xyz, search_radius, max_knn, selected_features):

@@ -626,6 +626,35 @@ int pgeof_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, const
                          (cudaStream_t)stream);
 }
 
+int pgeof_knn_features_f32(const float* xyz, int64_t n, uint32_t knn, const uint32_t* k_scales, int64_t n_scales,
+                           float* features, pgeof_stream_t stream) {
+    PGEOF_TRY(check_cloud(n, "xyz"));
+    if (knn == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "knn should be >= 1");
+    if ((int64_t)knn > n) return fail(PGEOF_ERR_INVALID_ARGUMENT, "knn size is greater than the data point cloud size");
+    if (n_scales < 0 || (n_scales > 0 && !k_scales) || !check_scales(k_scales, n_scales))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales should be > 1 and sorted in ascending order");
+    if (n_scales > 0 && k_scales[n_scales - 1] > knn)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales must not exceed knn");
+    if (n == 0) return PGEOF_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    GridIndex<float> grid;
+    PGEOF_TRY(build_grid<float>(xyz, (uint64_t)n, knn, 0.0f, 0.0f, grid, s));
+    // neighbour rows in cell order (no distances): the feature pass then walks
+    // spatially adjacent rows, whose neighbourhoods overlap in L1
+    Scratch nn, xyz4;
+    PGEOF_TRY(nn.alloc((size_t)n * knn * sizeof(uint32_t), s));
+    SearchOut<float> o;
+    o.indices = nn.p;
+    o.sqr_dist = nullptr;
+    o.rows_in_query_order = true;
+    PGEOF_TRY(launch_search<float>(grid, grid.pts, grid.cell_start, (uint64_t)n, MODE_KNN, knn, 0.0f, o, s));
+    PGEOF_TRY(xyz4.alloc((size_t)n * sizeof(float4), s));
+    PGEOF_TRY(pad_xyz(xyz, (uint64_t)n, xyz4.as<float4>(), s));
+    return launch_features(xyz4.as<float4>(), (uint64_t)n, nn.as<uint32_t>(), (uint64_t)n * knn, nullptr,
+                           (uint64_t)n, n_scales == 0, 1, k_scales, (int)n_scales, features, nullptr, s, nullptr, 0,
+                           grid.pts, knn);
+}
+
 int pgeof_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
                                        const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
                                        uint32_t k_min_search, float* features, pgeof_stream_t stream) {

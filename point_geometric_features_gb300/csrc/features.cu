@@ -48,6 +48,8 @@ struct FeatArgs {
     // its neighbour indices are local to that cloud's slice of xyz4
     const uint64_t* cloud_off;
     int n_clouds;
+    const SPoint<float>* row_map;  // optional: row r's output row is row_map[r].idx
+    uint32_t uniform_k;            // ptr == nullptr: row r is nn[r * uniform_k, (r + 1) * uniform_k)
 };
 
 struct RowCloud {
@@ -99,12 +101,19 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
     uint32_t flags = 0;
     unsigned n_resolved = 0;
     if (i < a.n_points) {
-        const uint32_t b = __ldg(a.ptr + i), e = __ldg(a.ptr + i + 1);
+        uint64_t b, e;
+        if (a.ptr) {
+            b = __ldg(a.ptr + i);
+            e = __ldg(a.ptr + i + 1);
+        } else {
+            b = (uint64_t)i * a.uniform_k;
+            e = b + a.uniform_k;
+        }
         uint32_t k_nn = 0;
-        if (e < b || (uint64_t)e > a.nnz) {
+        if (e < b || e > a.nnz) {
             flags |= ERR_PTR_RANGE;
         } else {
-            k_nn = e - b;
+            k_nn = (uint32_t)(e - b);
         }
         RowCloud rc{a.xyz4, a.n_xyz};
         if (MULTI) {
@@ -245,7 +254,15 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
     // coalesced write-out of the block's rows
     const uint32_t row0 = blockIdx.x * kFeatThreads;
     const uint32_t rows = min((uint32_t)kFeatThreads, a.n_points - row0);
-    if (a.n_scales == a.out_scales) {
+    if (a.row_map) {
+        // rows processed in another order: each row goes to its mapped output row
+        const int out_w = a.out_scales * 11;
+        for (int t = tid; t < (int)rows * row_w; t += kFeatThreads) {
+            const int r = t / row_w, c = t - r * row_w;
+            const uint64_t dst = a.row_map[row0 + r].idx;
+            a.out[dst * out_w + a.scale_offset * 11 + c] = stage[c * kFeatThreads + r];
+        }
+    } else if (a.n_scales == a.out_scales) {
         float* dst = a.out + (uint64_t)row0 * row_w;
         const int total = rows * row_w;
         for (int t = tid; t < total; t += kFeatThreads) {
@@ -539,9 +556,11 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off,
-                    int n_clouds) {
+                    int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k) {
     if (n_points == 0) return PGEOF_OK;
     FeatArgs a{};
+    a.row_map = row_map;
+    a.uniform_k = uniform_k;
     a.cloud_off = cloud_off;
     a.n_clouds = cloud_off ? n_clouds : 0;
     a.xyz4 = xyz4;

@@ -316,6 +316,12 @@ PYBIND11_MODULE(pgeof_ext, m) {
         check(pgeof_radius_search_csr_f32(P<const float>(data), n, P<const float>(query), m_, r, k, P<uint32_t>(nn),
                                           P<uint32_t>(nn_ptr), P<void>(stream)));
     });
+    m.def("_dev_knn_features", [](uintptr_t xyz, int64_t n, uint32_t knn, std::vector<uint32_t> scales,
+                                  uintptr_t out, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_knn_features_f32(P<const float>(xyz), n, knn, scales.data(), (int64_t)scales.size(),
+                                     P<float>(out), P<void>(stream)));
+    });
     m.def("_dev_compute_features", [](uintptr_t xyz, int64_t n_xyz, uintptr_t nn, int64_t nnz, uintptr_t ptr,
                                       int64_t n, uint64_t k_min, uintptr_t out, uintptr_t stream) {
         py::gil_scoped_release nogil;

@@ -112,6 +112,7 @@ struct SearchArgs {
     T* out_d2;
     uint32_t* out_found;
     int fill_last;
+    int rows_sorted;  // output row = position in `queries`
     uint32_t* err;
 };
 
@@ -531,8 +532,8 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
         int P = 1;
         while (P < (int)n_sel) P <<= 1;
         if (n_sel > 1) bitonic_sort<T>(buf, (int)n_sel, P);
-        emit_row<T>(a.mode, k, n_sel, found, row_base + qp.idx, a.out_idx, a.out_d2, a.out_found, a.fill_last, a.r2,
-                    [&](uint32_t j) { return buf[j]; });
+        emit_row<T>(a.mode, k, n_sel, found, a.rows_sorted ? qpos : row_base + qp.idx, a.out_idx, a.out_d2,
+                    a.out_found, a.fill_last, a.r2, [&](uint32_t j) { return buf[j]; });
         __syncwarp();
     }
 }
@@ -566,6 +567,7 @@ struct FastArgs {
     float* out_d2;
     uint32_t* out_found;
     int fill_last;
+    int rows_sorted;  // output row = position in `queries`
     uint32_t* err;
 };
 
@@ -772,8 +774,8 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                 }
                 continue;
             }
-            emit_row<float>(a.mode, k, n_sel, count, row_base + qp.idx, a.out_idx, a.out_d2, a.out_found,
-                            a.fill_last, a.r2,
+            emit_row<float>(a.mode, k, n_sel, count, a.rows_sorted ? qi : row_base + qp.idx, a.out_idx, a.out_d2,
+                            a.out_found, a.fill_last, a.r2,
                             [&](uint32_t j) {
                                 const uint64_t key = sorted[j];
                                 Entry<float> e;
@@ -916,6 +918,7 @@ int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoin
     a.out_d2 = out.sqr_dist;
     a.out_found = out.found;
     a.fill_last = out.radius_fill_last ? 1 : 0;
+    a.rows_sorted = out.rows_in_query_order ? 1 : 0;
     a.err = device_error_word();
     KernelTimer kt(qlist ? "overflow_search_kernel" : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel"),
                    s);
@@ -977,6 +980,7 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     a.out_d2 = out.sqr_dist;
     a.out_found = out.found;
     a.fill_last = out.radius_fill_last ? 1 : 0;
+    a.rows_sorted = out.rows_in_query_order ? 1 : 0;
     a.err = device_error_word();
     {
         KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);

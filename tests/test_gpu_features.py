@@ -198,3 +198,31 @@ def test_full_size_multiscale_properties(cuda, pgeof):
     sub_ptr = (np.arange(rows.size + 1) * 50).astype(np.uint32)
     ref = oracle.compute_features_multiscale(xyz, sub_nn, sub_ptr, [10, 20, 50])
     _assert_features(m[rows], ref)
+
+
+@pytest.mark.parametrize("k", [8, 50])
+def test_knn_features_equals_separate_calls(cuda, pgeof, k):
+    """The fused feature-only pipeline writes exactly what knn_search followed
+    by compute_features / compute_features_multiscale writes."""
+    torch = cuda
+    for xyz in (outdoor_scene(60_000, seed=21), uniform_cube(30_000, seed=22)):
+        t = torch.from_numpy(xyz).cuda()
+        idx, _ = pgeof.knn_search(t, t, k)
+        ptr = torch.arange(0, k * (xyz.shape[0] + 1), k, dtype=torch.int32, device="cuda")
+        ref = pgeof.compute_features(t, idx.reshape(-1), ptr)
+        got = pgeof.knn_features(t, k)
+        assert torch.equal(got, ref)
+        scales = [max(1, k // 4), k // 2, k]
+        ref3 = pgeof.compute_features_multiscale(t, idx.reshape(-1), ptr, scales)
+        got3 = pgeof.knn_features(t, k, scales)
+        assert torch.equal(got3, ref3)
+    # numpy in, numpy out
+    small = uniform_cube(2_000, seed=23)
+    got = pgeof.knn_features(small, 10)
+    i, _ = pgeof.knn_search(small, small, 10)
+    ref = pgeof.compute_features(small, i.reshape(-1), (np.arange(2_001) * 10).astype(np.uint32))
+    np.testing.assert_array_equal(got, ref)
+    with pytest.raises(ValueError):
+        pgeof.knn_features(small, 2_001)
+    with pytest.raises(ValueError):
+        pgeof.knn_features(small, 10, [5, 20])
