@@ -93,6 +93,16 @@ cudaStream_t host_stream() {
     return streams[dev];
 }
 
+// Copy streams of the host-pointer API's feature pipeline (0: uploads, 1:
+// downloads), one pair per host thread and device.
+cudaStream_t host_copy_stream(int which) {
+    thread_local cudaStream_t streams[2][kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!streams[which][dev]) cudaStreamCreateWithFlags(&streams[which][dev], cudaStreamNonBlocking);
+    return streams[which][dev];
+}
+
 // Per-call data-error word for host-pointer calls (no cross-talk between threads).
 struct CallErrors {
     Scratch word;
@@ -744,14 +754,76 @@ static int host_features(const float* xyz, int64_t n_xyz, const uint32_t* nn, in
     PGEOF_TRY(ce.begin());
     Scratch d_xyz, d_nn, d_ptr, d_out;
     PGEOF_TRY(upload(d_xyz, xyz, 3ull * n_xyz, s));
-    PGEOF_TRY(upload(d_nn, nn, (uint64_t)nnz, s));
     PGEOF_TRY(upload(d_ptr, nn_ptr, (uint64_t)n_points + 1, s));
     const uint64_t cnt = (uint64_t)n_points * row_width;
     PGEOF_TRY(d_out.alloc(cnt * sizeof(float), s));
-    PGEOF_TRY(features_impl(d_xyz.as<float>(), n_xyz, d_nn.as<uint32_t>(), nnz, d_ptr.as<uint32_t>(), n_points, kind,
-                            k_min, scales, n_scales, k_step, k_min_search, d_out.as<float>(), s));
-    PGEOF_TRY(download(features, d_out, cnt, s));
-    return finish_host(ce, s);
+    const uint64_t nn_bytes = (uint64_t)nnz * sizeof(uint32_t);
+    if (kind == 2 || nn_bytes < (64ull << 20) || n_points < 1024) {
+        PGEOF_TRY(upload(d_nn, nn, (uint64_t)nnz, s));
+        PGEOF_TRY(features_impl(d_xyz.as<float>(), n_xyz, d_nn.as<uint32_t>(), nnz, d_ptr.as<uint32_t>(), n_points,
+                                kind, k_min, scales, n_scales, k_step, k_min_search, d_out.as<float>(), s));
+        PGEOF_TRY(download(features, d_out, cnt, s));
+        return finish_host(ce, s);
+    }
+    // Large neighbour lists: rows in chunks, so that chunk c's neighbour upload,
+    // chunk c-1's feature pass and chunk c-2's result download overlap. A chunk's
+    // rows read only its own slice nn[nn_ptr[r0], nn_ptr[r1]) when nn_ptr is
+    // non-decreasing (anything else is reported by the kernel as a data error);
+    // the slices are clamped to len(nn) on the host.
+    PGEOF_TRY(d_nn.alloc(nn_bytes, s));
+    Scratch xyz4;
+    PGEOF_TRY(xyz4.alloc(std::max<uint64_t>(n_xyz, 1) * sizeof(float4), s));
+    PGEOF_TRY(pad_xyz(d_xyz.as<float>(), n_xyz, xyz4.as<float4>(), s));
+    const cudaStream_t cin = host_copy_stream(0), cout = host_copy_stream(1);
+    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, nn_bytes / (24ull << 20)));
+    std::vector<cudaEvent_t> ev(2 * C + 3, nullptr);  // start, (upload, kernel) per chunk, 2 final
+    for (auto& e : ev) PGEOF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    int status = PGEOF_OK;
+    const uint64_t n = (uint64_t)n_points, total = (uint64_t)nnz;
+    do {
+        // scratch allocated on s must exist before the copy streams touch it
+        if (cudaEventRecord(ev[0], s) != cudaSuccess || cudaStreamWaitEvent(cin, ev[0], 0) != cudaSuccess ||
+            cudaStreamWaitEvent(cout, ev[0], 0) != cudaSuccess) {
+            status = fail(PGEOF_ERR_CUDA, "feature pipeline: stream ordering failed");
+            break;
+        }
+        for (int c = 0; c < C && status == PGEOF_OK; ++c) {
+            const uint64_t r0 = n * c / C, r1 = n * (c + 1) / C;
+            if (r1 == r0) continue;
+            const uint64_t lo = std::min<uint64_t>(nn_ptr[r0], total);
+            const uint64_t hi = std::min<uint64_t>(std::max<uint64_t>(nn_ptr[r1], lo), total);
+            if (hi > lo &&
+                cudaMemcpyAsync(d_nn.as<uint32_t>() + lo, nn + lo, (hi - lo) * sizeof(uint32_t),
+                                cudaMemcpyHostToDevice, cin) != cudaSuccess) {
+                status = fail(PGEOF_ERR_CUDA, "feature pipeline: upload failed");
+                break;
+            }
+            if (cudaEventRecord(ev[1 + 2 * c], cin) != cudaSuccess ||
+                cudaStreamWaitEvent(s, ev[1 + 2 * c], 0) != cudaSuccess) {
+                status = fail(PGEOF_ERR_CUDA, "feature pipeline: stream ordering failed");
+                break;
+            }
+            status = launch_features(xyz4.as<float4>(), n_xyz, d_nn.as<uint32_t>(), total, d_ptr.as<uint32_t>(),
+                                     r1 - r0, kind == 0, k_min, scales, (int)n_scales, d_out.as<float>(), nullptr, s,
+                                     nullptr, 0, nullptr, 0, r0);
+            if (status != PGEOF_OK) break;
+            if (cudaEventRecord(ev[2 + 2 * c], s) != cudaSuccess ||
+                cudaStreamWaitEvent(cout, ev[2 + 2 * c], 0) != cudaSuccess ||
+                cudaMemcpyAsync(features + r0 * row_width, d_out.as<float>() + r0 * row_width,
+                                (r1 - r0) * row_width * sizeof(float), cudaMemcpyDeviceToHost, cout) != cudaSuccess) {
+                status = fail(PGEOF_ERR_CUDA, "feature pipeline: download failed");
+                break;
+            }
+        }
+    } while (false);
+    // the scratch is released on s: let s wait for both copy streams
+    cudaEventRecord(ev[2 * C + 1], cin);
+    cudaEventRecord(ev[2 * C + 2], cout);
+    cudaStreamWaitEvent(s, ev[2 * C + 1], 0);
+    cudaStreamWaitEvent(s, ev[2 * C + 2], 0);
+    const int fin = finish_host(ce, s);
+    for (auto& e : ev) cudaEventDestroy(e);
+    return status != PGEOF_OK ? status : fin;
 }
 
 int pgeof_host_compute_features_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,

@@ -50,6 +50,7 @@ struct FeatArgs {
     int n_clouds;
     const SPoint<float>* row_map;  // optional: row r's output row is row_map[r].idx
     uint32_t uniform_k;            // ptr == nullptr: row r is nn[r * uniform_k, (r + 1) * uniform_k)
+    uint32_t row_base;             // this launch covers rows [row_base, row_base + n_points)
 };
 
 struct RowCloud {
@@ -94,13 +95,13 @@ template <int S, bool MULTI>
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
     extern __shared__ float stage[];  // kFeatThreads * n_scales * 11
     const int tid = threadIdx.x;
-    const uint32_t i = blockIdx.x * kFeatThreads + tid;
+    const uint32_t i = a.row_base + blockIdx.x * kFeatThreads + tid;
     const int row_w = a.n_scales * 11;
     for (int f = 0; f < row_w; ++f) stage[f * kFeatThreads + tid] = 0.0f;  // column-major staging
 
     uint32_t flags = 0;
     unsigned n_resolved = 0;
-    if (i < a.n_points) {
+    if (i < a.row_base + a.n_points) {
         uint64_t b, e;
         if (a.ptr) {
             b = __ldg(a.ptr + i);
@@ -252,8 +253,8 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
     if (a.resolved && n_resolved) atomicAdd(a.resolved, (unsigned long long)n_resolved);
     __syncthreads();
     // coalesced write-out of the block's rows
-    const uint32_t row0 = blockIdx.x * kFeatThreads;
-    const uint32_t rows = min((uint32_t)kFeatThreads, a.n_points - row0);
+    const uint32_t row0 = a.row_base + blockIdx.x * kFeatThreads;
+    const uint32_t rows = min((uint32_t)kFeatThreads, a.row_base + a.n_points - row0);
     if (a.row_map) {
         // rows processed in another order: each row goes to its mapped output row
         const int out_w = a.out_scales * 11;
@@ -556,11 +557,12 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off,
-                    int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k) {
+                    int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k, uint64_t row_base) {
     if (n_points == 0) return PGEOF_OK;
     FeatArgs a{};
     a.row_map = row_map;
     a.uniform_k = uniform_k;
+    a.row_base = (uint32_t)row_base;
     a.cloud_off = cloud_off;
     a.n_clouds = cloud_off ? n_clouds : 0;
     a.xyz4 = xyz4;

@@ -226,3 +226,26 @@ def test_knn_features_equals_separate_calls(cuda, pgeof, k):
         pgeof.knn_features(small, 2_001)
     with pytest.raises(ValueError):
         pgeof.knn_features(small, 10, [5, 20])
+
+
+def test_host_pipeline_large_csr_matches_device_path(cuda, pgeof):
+    """Neighbour lists of >= 64 MB go through the chunked host pipeline (upload,
+    feature pass and download of successive row chunks overlapped); results
+    must equal the device path's, and bad offsets still raise."""
+    torch = cuda
+    n, k = 400_000, 50
+    xyz = outdoor_scene(n, seed=31)
+    t = torch.from_numpy(xyz).cuda()
+    idx, _ = pgeof.knn_search(t, t, k)
+    nn_h = idx.cpu().numpy().astype(np.uint32).reshape(-1)
+    assert nn_h.nbytes >= 64 << 20
+    ptr_h = (np.arange(n + 1, dtype=np.int64) * k).astype(np.uint32)
+    ptr_d = torch.from_numpy(ptr_h.view(np.int32)).cuda()
+    ref1 = pgeof.compute_features(t, idx.reshape(-1), ptr_d).cpu().numpy()
+    np.testing.assert_array_equal(pgeof.compute_features(xyz, nn_h, ptr_h), ref1)
+    ref3 = pgeof.compute_features_multiscale(t, idx.reshape(-1), ptr_d, [10, 20, 50]).cpu().numpy()
+    np.testing.assert_array_equal(pgeof.compute_features_multiscale(xyz, nn_h, ptr_h, [10, 20, 50]), ref3)
+    bad = ptr_h.copy()
+    bad[n // 2] = bad[n // 2 + 1] + 7  # a decreasing step in the middle chunk
+    with pytest.raises(ValueError):
+        pgeof.compute_features(xyz, nn_h, bad)
