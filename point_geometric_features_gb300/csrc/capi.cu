@@ -714,11 +714,52 @@ int pgeof_host_knn_search_f32(const float* data, int64_t n_data, const float* qu
     const uint64_t cnt = (uint64_t)n_query * knn;
     PGEOF_TRY(d_idx.alloc(cnt * sizeof(uint32_t), s));
     PGEOF_TRY(d_d2.alloc(cnt * sizeof(float), s));
-    PGEOF_TRY(knn_impl(d_data.as<float>(), n_data, same ? d_data.as<float>() : d_query.as<float>(), n_query, knn,
-                       d_idx.as<uint32_t>(), d_d2.as<float>(), same, s));
-    PGEOF_TRY(download(indices, d_idx, cnt, s));
-    PGEOF_TRY(download(sqr_dist, d_d2, cnt, s));
-    return finish_host(ce, s);
+    const uint64_t out_bytes = cnt * (sizeof(uint32_t) + sizeof(float));
+    if (out_bytes < (128ull << 20) || n_query < 65536) {
+        PGEOF_TRY(knn_impl(d_data.as<float>(), n_data, same ? d_data.as<float>() : d_query.as<float>(), n_query, knn,
+                           d_idx.as<uint32_t>(), d_d2.as<float>(), same, s));
+        PGEOF_TRY(download(indices, d_idx, cnt, s));
+        PGEOF_TRY(download(sqr_dist, d_d2, cnt, s));
+        return finish_host(ce, s);
+    }
+    // Large results: the queries in chunks of consecutive rows, each sorted into
+    // cell order and searched against the one grid, so that chunk c's rows
+    // download while chunk c+1 is searched.
+    GridIndex<float> grid;
+    PGEOF_TRY(build_grid<float>(d_data.as<float>(), (uint64_t)n_data, knn, 0.0f, 0.0f, grid, s));
+    const float* qbase = same ? d_data.as<float>() : d_query.as<float>();
+    const cudaStream_t cout = host_copy_stream(1);
+    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, out_bytes / (96ull << 20)));
+    std::vector<cudaEvent_t> ev(C + 2, nullptr);  // start, one per chunk, final
+    for (auto& e : ev) PGEOF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    int status = PGEOF_OK;
+    Scratch qmem, qstart_mem;
+    const uint64_t m = (uint64_t)n_query;
+    if (cudaEventRecord(ev[0], s) != cudaSuccess || cudaStreamWaitEvent(cout, ev[0], 0) != cudaSuccess)
+        status = fail(PGEOF_ERR_CUDA, "knn pipeline: stream ordering failed");
+    for (int c = 0; c < C && status == PGEOF_OK; ++c) {
+        const uint64_t r0 = m * c / C, r1 = m * (c + 1) / C;
+        if (r1 == r0) continue;
+        SPoint<float>* qs = nullptr;
+        status = sort_queries<float>(qbase + 3 * r0, r1 - r0, grid.g, qmem, &qs, qstart_mem, s);
+        if (status != PGEOF_OK) break;
+        SearchOut<float> o;
+        o.indices = d_idx.as<uint32_t>() + r0 * knn;
+        o.sqr_dist = d_d2.as<float>() + r0 * knn;
+        status = launch_search<float>(grid, qs, qstart_mem.as<uint32_t>(), r1 - r0, MODE_KNN, knn, 0.0f, o, s);
+        if (status != PGEOF_OK) break;
+        if (cudaEventRecord(ev[1 + c], s) != cudaSuccess || cudaStreamWaitEvent(cout, ev[1 + c], 0) != cudaSuccess ||
+            cudaMemcpyAsync(indices + r0 * knn, d_idx.as<uint32_t>() + r0 * knn, (r1 - r0) * knn * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, cout) != cudaSuccess ||
+            cudaMemcpyAsync(sqr_dist + r0 * knn, d_d2.as<float>() + r0 * knn, (r1 - r0) * knn * sizeof(float),
+                            cudaMemcpyDeviceToHost, cout) != cudaSuccess)
+            status = fail(PGEOF_ERR_CUDA, "knn pipeline: download failed");
+    }
+    cudaEventRecord(ev[C + 1], cout);
+    cudaStreamWaitEvent(s, ev[C + 1], 0);
+    const int fin = finish_host(ce, s);
+    for (auto& e : ev) cudaEventDestroy(e);
+    return status != PGEOF_OK ? status : fin;
 }
 
 int pgeof_host_radius_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,

@@ -216,3 +216,23 @@ def test_radius_search_csr_edges(cuda, pgeof):
     ref_nn, ref_ptr = _csr_from_table(idx.cpu().numpy())
     ref = pgeof.compute_features_optimal(xyz.cpu().numpy(), ref_nn, ref_ptr, 1, 1, 5)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_host_knn_pipeline_large_matches_device_path(cuda, pgeof):
+    """Results of >= 128 MB take the chunked host path (query row chunks sorted
+    and searched in turn, downloads overlapped): identical to the device path,
+    for the cloud itself and for separate queries."""
+    torch = cuda
+    xyz = outdoor_scene(400_000, seed=41)
+    t = torch.from_numpy(xyz).cuda()
+    i_d, d_d = pgeof.knn_search(t, t, 50)
+    i_h, d_h = pgeof.knn_search(xyz, xyz, 50)
+    np.testing.assert_array_equal(i_h, i_d.cpu().numpy().astype(np.uint32))
+    np.testing.assert_array_equal(d_h, d_d.cpu().numpy())
+    q = uniform_cube(420_000, seed=42, side=100.0)
+    q[:, 2] *= 0.2
+    qt = torch.from_numpy(q).cuda()
+    i_d, d_d = pgeof.knn_search(t, qt, 40)
+    i_h, d_h = pgeof.knn_search(xyz, q, 40)
+    np.testing.assert_array_equal(i_h, i_d.cpu().numpy().astype(np.uint32))
+    np.testing.assert_array_equal(d_h, d_d.cpu().numpy())
