@@ -609,18 +609,21 @@ __device__ __forceinline__ void bitonic_keys(uint64_t* keys, int n, int P) {
 // key. Returns false, writing nothing, when those bins hold more than out_cap
 // keys.
 __device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* keys, uint32_t count,
-                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t out_cap) {
+                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t out_cap,
+                                              bool hist_ready = false) {
     const int lane = threadIdx.x & 31;
     const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
-    ws->hist[lane] = 0;
-    ws->hist[lane + 32] = 0;
-    __syncwarp();
-    for (uint32_t i = lane; i < count; i += 32) {
-        const float x = key_d2(keys[i]) * sb;
-        const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
-        atomicAdd(&ws->hist[bin], 1u);
+    if (!hist_ready) {
+        ws->hist[lane] = 0;
+        ws->hist[lane + 32] = 0;
+        __syncwarp();
+        for (uint32_t i = lane; i < count; i += 32) {
+            const float x = key_d2(keys[i]) * sb;
+            const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
+            atomicAdd(&ws->hist[bin], 1u);
+        }
+        __syncwarp();
     }
-    __syncwarp();
     // lane owns bins 2*lane, 2*lane+1
     const uint32_t h0 = ws->hist[2 * lane], h1 = ws->hist[2 * lane + 1];
     uint32_t incl = h0 + h1;
@@ -752,6 +755,11 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             const float tf = sqrtf(tau2) * 1.000001f + g.margin;
             const Box rb = region_box(g, q[0], q[1], q[2], tf);
             uint32_t count = 0;
+            // the selection histogram is filled while collecting
+            const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
+            ws->hist[lane] = 0;
+            ws->hist[lane + 32] = 0;
+            __syncwarp();
             visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
                              [&](bool valid, float d2, uint32_t idx) {
                                  const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
@@ -759,6 +767,8 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                                  if (take) {
                                      const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
                                      if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                                     const float x = d2 * sb;
+                                     atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
                                  }
                                  count += __popc(mask);
                              });
@@ -766,7 +776,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             const bool short_knn = a.mode == MODE_KNN && count < k;  // rounding corner: never expected
             const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
             const bool ok = count <= a.cap && !short_knn &&
-                            (n_sel == 0 || select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted));
+                            (n_sel == 0 || select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, true));
             if (!ok) {
                 if (lane == 0) {
                     const uint32_t slot = atomicAdd(a.ovf_count, 1u);
