@@ -315,9 +315,13 @@ struct KSum {
 };
 
 // Eigenvalues of a symmetric 3x3 by the trigonometric closed form (O. K.
-// Smith, "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961). Used only to
-// rank candidate neighbourhood sizes.
-__device__ __forceinline__ void eigvals_closed_form(const Cov<float>& c, float (&w)[3]) {
+// Smith, "Eigenvalues of a symmetric 3x3 matrix", CACM 4(4), 1961), used only
+// to rank candidate neighbourhood sizes. The scan ranks candidate sizes and every size within
+// kTieBand (3e-5) of its minimum is re-evaluated exactly, so the scan's values
+// need only stay within half the band of the exact ones. The hardware cosine
+// and logarithm (__cosf: absolute error < 2^-21 on [-pi, pi]; __logf) add about
+// 1e-6 to the eigentropy -- well inside it.
+__device__ __forceinline__ void eigvals_closed_form_scan(const Cov<float>& c, float (&w)[3]) {
     const float q = (c.xx + c.yy + c.zz) * (1.0f / 3.0f);
     const float b00 = c.xx - q, b11 = c.yy - q, b22 = c.zz - q;
     const float off = c.xy * c.xy + c.xz * c.xz + c.yz * c.yz;
@@ -329,14 +333,22 @@ __device__ __forceinline__ void eigvals_closed_form(const Cov<float>& c, float (
     const float p = sqrtf(p2);
     const float det = b00 * (b11 * b22 - c.yz * c.yz) - c.xy * (c.xy * b22 - c.yz * c.xz) +
                       c.xz * (c.xy * c.yz - b11 * c.xz);
-    float r = det / (2.0f * p2 * p);
+    float r = __fdividef(det, 2.0f * p2 * p);
     r = fminf(1.0f, fmaxf(-1.0f, r));
     const float phi = acosf(r) * (1.0f / 3.0f);
-    const float e2 = q + 2.0f * p * cosf(phi);
-    const float e0 = q + 2.0f * p * cosf(phi + 2.0943951023931953f);
+    const float e2 = q + 2.0f * p * __cosf(phi);
+    const float e0 = q + 2.0f * p * __cosf(phi + 2.0943951023931953f);
     w[0] = e0;
     w[2] = e2;
     w[1] = 3.0f * q - e0 - e2;
+}
+
+// include/pca.hpp:140-150 with the hardware logarithm (scan ranking only).
+__device__ __forceinline__ float eigentropy_scan(const float (&val)[3]) {
+    const float eps = 1e-3f;
+    const float inv = __fdividef(1.0f, val[0] + val[1] + val[2] + eps);
+    const float e0 = val[0] * inv, e1 = val[1] * inv, e2 = val[2] * inv;
+    return -(e0 * __logf(e0 + eps) + e1 * __logf(e1 + eps) + e2 * __logf(e2 + eps));
 }
 
 // Covariance of the first k neighbours exactly as include/pca.hpp:75-76.
@@ -451,11 +463,11 @@ __global__ void __launch_bounds__(kOptThreads) optimal_kernel(const __grid_const
                 c.yz = syz.s * inv - my * mz;
                 c.zz = szz.s * inv - mz * mz;
                 float w[3];
-                eigvals_closed_form(c, w);
+                eigvals_closed_form_scan(c, w);
                 float val[3];
 #pragma unroll
                 for (int q = 0; q < 3; ++q) val[q] = fmaxf(w[a.order ? 2 - q : q], 0.0f);
-                const float ent_k = eigentropy_of<float>(val);
+                const float ent_k = eigentropy_scan(val);
                 if (k == k0 || ent_k < best) best = ent_k;
                 if (slot < kOptSlots) {
                     ent[slot * kOptThreads + tid] = ent_k;
