@@ -58,38 +58,39 @@ struct RowCloud {
     uint32_t n;
 };
 
-__device__ __forceinline__ float4 gather_nb(const RowCloud& rc, uint32_t id, uint32_t& flags) {
-    if (id >= rc.n) {
+__device__ __forceinline__ float4 gather_nb(const float4* xyz4, uint32_t n_xyz, uint32_t id, uint32_t& flags) {
+    if (id >= n_xyz) {
         flags |= ERR_NN_RANGE;
         id = 0;
     }
-    return __ldg(rc.xyz4 + id);
+    return __ldg(xyz4 + id);
 }
 
-// Calls f(j, point) for the row's neighbours j = 0 .. kmax-1 in order. Indices
-// are read four at a time (16-byte loads once the row pointer is aligned),
-// which quarters the L1 requests for them, and each group's four gathers are
-// issued before any is used.
+// Calls f(j, point) for the neighbours j = 0 .. count-1 of the CSR row at
+// nn + b, in order. Indices are read four at a time (16-byte loads once the
+// row pointer is aligned), which quarters the L1 requests for them, and each
+// group's four gathers are issued before any is used.
 template <typename F>
-__device__ __forceinline__ void for_each_nb(const FeatArgs& a, const RowCloud& rc, uint64_t b, uint32_t kmax,
-                                            uint32_t& flags, F&& f) {
-    const uint32_t* nn = a.nn + b;
+__device__ __forceinline__ void gather_row(const uint32_t* nn_all, uint64_t b, uint32_t count, const float4* xyz4,
+                                           uint32_t n_xyz, uint32_t& flags, F&& f) {
+    const uint32_t* nn = nn_all + b;
     uint32_t j = 0;
-    while (j < kmax && (reinterpret_cast<uintptr_t>(nn + j) & 15u)) {
-        f(j, gather_nb(rc, __ldg(nn + j), flags));
+    while (j < count && (reinterpret_cast<uintptr_t>(nn + j) & 15u)) {
+        f(j, gather_nb(xyz4, n_xyz, __ldg(nn + j), flags));
         ++j;
     }
-    for (; j + 4 <= kmax; j += 4) {
+    for (; j + 4 <= count; j += 4) {
         const uint4 ids = __ldg(reinterpret_cast<const uint4*>(nn + j));
-        const float4 p0 = gather_nb(rc, ids.x, flags), p1 = gather_nb(rc, ids.y, flags);
-        const float4 p2 = gather_nb(rc, ids.z, flags), p3 = gather_nb(rc, ids.w, flags);
+        const float4 p0 = gather_nb(xyz4, n_xyz, ids.x, flags), p1 = gather_nb(xyz4, n_xyz, ids.y, flags);
+        const float4 p2 = gather_nb(xyz4, n_xyz, ids.z, flags), p3 = gather_nb(xyz4, n_xyz, ids.w, flags);
         f(j, p0);
         f(j + 1, p1);
         f(j + 2, p2);
         f(j + 3, p3);
     }
-    for (; j < kmax; ++j) f(j, gather_nb(rc, __ldg(nn + j), flags));
+    for (; j < count; ++j) f(j, gather_nb(xyz4, n_xyz, __ldg(nn + j), flags));
 }
+
 
 template <int S, bool MULTI>
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
@@ -152,48 +153,53 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             float mx[S], my[S], mz[S];
 #pragma unroll
             for (int s = 0; s < S; ++s) mx[s] = my[s] = mz[s] = 0.0f;
-            for_each_nb(a, rc, b, kmax, flags, [&](uint32_t j, const float4& p) {
-                rx = FADD(rx, p.x);
-                ry = FADD(ry, p.y);
-                rz = FADD(rz, p.z);
-                if constexpr (S > 1) {
+            // both sweeps run in segments [ks[t-1], ks[t]) between the (ascending)
+            // scale sizes, so each neighbour updates only the scales that contain it
+            uint32_t j0 = 0;
 #pragma unroll
-                    for (int s = 0; s < S; ++s) {
-                        if (s < n_active && j + 1 == ks[s]) {
-                            const float kk = (float)ks[s];
-                            mx[s] = FDIV(rx, kk);
-                            my[s] = FDIV(ry, kk);
-                            mz[s] = FDIV(rz, kk);
-                        }
-                    }
+            for (int t = 0; t < S; ++t) {
+                if (t < n_active) {
+                    const uint32_t j1 = ks[t];
+                    gather_row(a.nn, b + j0, j1 - j0, rc.xyz4, rc.n, flags, [&](uint32_t, const float4& p) {
+                        rx = FADD(rx, p.x);
+                        ry = FADD(ry, p.y);
+                        rz = FADD(rz, p.z);
+                    });
+                    const float kk = (float)j1;
+                    mx[t] = FDIV(rx, kk);
+                    my[t] = FDIV(ry, kk);
+                    mz[t] = FDIV(rz, kk);
+                    j0 = j1;
                 }
-            });
-            if constexpr (S == 1) {
-                const float kk = (float)ks[0];
-                mx[0] = FDIV(rx, kk);
-                my[0] = FDIV(ry, kk);
-                mz[0] = FDIV(rz, kk);
             }
             // sweep 2: centred products, sequential sums
             float cxx[S], cxy[S], cxz[S], cyy[S], cyz[S], czz[S];
 #pragma unroll
             for (int s = 0; s < S; ++s) cxx[s] = cxy[s] = cxz[s] = cyy[s] = cyz[s] = czz[s] = 0.0f;
-            for_each_nb(a, rc, b, kmax, flags, [&](uint32_t j, const float4& p) {
+            j0 = 0;
 #pragma unroll
-                for (int s = 0; s < S; ++s) {
-                    if (s < n_active && j < ks[s]) {
-                        const float dx = FSUB(p.x, mx[s]);
-                        const float dy = FSUB(p.y, my[s]);
-                        const float dz = FSUB(p.z, mz[s]);
-                        cxx[s] = FADD(cxx[s], FMUL(dx, dx));
-                        cxy[s] = FADD(cxy[s], FMUL(dx, dy));
-                        cxz[s] = FADD(cxz[s], FMUL(dx, dz));
-                        cyy[s] = FADD(cyy[s], FMUL(dy, dy));
-                        cyz[s] = FADD(cyz[s], FMUL(dy, dz));
-                        czz[s] = FADD(czz[s], FMUL(dz, dz));
-                    }
+            for (int t = 0; t < S; ++t) {
+                if (t < n_active) {
+                    const uint32_t j1 = ks[t];
+                    gather_row(a.nn, b + j0, j1 - j0, rc.xyz4, rc.n, flags, [&](uint32_t, const float4& p) {
+#pragma unroll
+                        for (int s = t; s < S; ++s) {
+                            if (s < n_active) {
+                                const float dx = FSUB(p.x, mx[s]);
+                                const float dy = FSUB(p.y, my[s]);
+                                const float dz = FSUB(p.z, mz[s]);
+                                cxx[s] = FADD(cxx[s], FMUL(dx, dx));
+                                cxy[s] = FADD(cxy[s], FMUL(dx, dy));
+                                cxz[s] = FADD(cxz[s], FMUL(dx, dz));
+                                cyy[s] = FADD(cyy[s], FMUL(dy, dy));
+                                cyz[s] = FADD(cyz[s], FMUL(dy, dz));
+                                czz[s] = FADD(czz[s], FMUL(dz, dz));
+                            }
+                        }
+                    });
+                    j0 = j1;
                 }
-            });
+            }
             if constexpr (S == 1) {
                 const float kk = (float)ks[0];
                 Cov<float> c;
@@ -353,14 +359,10 @@ __device__ __forceinline__ float eigentropy_scan(const float (&val)[3]) {
 
 // Covariance of the first k neighbours exactly as include/pca.hpp:75-76.
 __device__ __forceinline__ Cov<float> literal_cov(const OptArgs& a, uint32_t b, uint32_t k, uint32_t& flags) {
+    // scalar index loads here: the 4-wide form costs this kernel ~20 registers
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
     for (uint32_t j = 0; j < k; ++j) {
-        uint32_t id = __ldg(a.nn + b + j);
-        if (id >= a.n_xyz) {
-            flags |= ERR_NN_RANGE;
-            id = 0;
-        }
-        const float4 p = __ldg(a.xyz4 + id);
+        const float4 p = gather_nb(a.xyz4, a.n_xyz, __ldg(a.nn + b + j), flags);
         sx = FADD(sx, p.x);
         sy = FADD(sy, p.y);
         sz = FADD(sz, p.z);
@@ -369,9 +371,7 @@ __device__ __forceinline__ Cov<float> literal_cov(const OptArgs& a, uint32_t b, 
     const float mx = FDIV(sx, kk), my = FDIV(sy, kk), mz = FDIV(sz, kk);
     float xx = 0.0f, xy = 0.0f, xz = 0.0f, yy = 0.0f, yz = 0.0f, zz = 0.0f;
     for (uint32_t j = 0; j < k; ++j) {
-        uint32_t id = __ldg(a.nn + b + j);
-        if (id >= a.n_xyz) id = 0;
-        const float4 p = __ldg(a.xyz4 + id);
+        const float4 p = gather_nb(a.xyz4, a.n_xyz, __ldg(a.nn + b + j), flags);
         const float dx = FSUB(p.x, mx), dy = FSUB(p.y, my), dz = FSUB(p.z, mz);
         xx = FADD(xx, FMUL(dx, dx));
         xy = FADD(xy, FMUL(dx, dy));
@@ -436,12 +436,7 @@ __global__ void __launch_bounds__(kOptThreads) optimal_kernel(const __grid_const
             int slot = 0;
             bool stored_all = true;
             for (uint32_t k = 1; k <= k_nn; ++k) {
-                uint32_t id = __ldg(a.nn + b + k - 1);
-                if (id >= a.n_xyz) {
-                    flags |= ERR_NN_RANGE;
-                    id = 0;
-                }
-                const float4 p = __ldg(a.xyz4 + id);
+                const float4 p = gather_nb(a.xyz4, a.n_xyz, __ldg(a.nn + b + k - 1), flags);
                 const float dx = p.x - p0.x, dy = p.y - p0.y, dz = p.z - p0.z;
                 s1x.add(dx);
                 s1y.add(dy);
