@@ -65,6 +65,8 @@ def parse():
                    help="scene: the headline 1M-point kNN+multiscale step; features: the 1M-point k=50 "
                         "compute_features pass alone; batch: 256 clouds, plain vs batched; serve: Poisson request "
                         "stream with p50/p99 latency; optimal: 4M-point radius -> optimal-k")
+    p.add_argument("--points", type=int, default=None,
+                   help="scene / features: cloud size (default 1,000,000; e.g. 4M and 16M for the asymptote)")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
     return p.parse_args()
@@ -291,7 +293,7 @@ def run_ours(args, rank, world, local):
                         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                         "algorithmic_bytes_per_launch": algo * N_POINTS,
                         "avg_launch_ms": round(kms / n, 4),
-                        "traffic": traffic_from_profile()}
+                        "traffic": (traffic_from_profile() or 0) * N_POINTS / 1e6 or None}
     value = world * N_POINTS * args.steps / (total_ms / 1e3)
     line = {
         "metric": METRIC,
@@ -611,8 +613,12 @@ def run_features(args):
 
 
 def main():
+    global N_POINTS, WORKLOAD
     args = parse()
     rank, world, local = dist_env()
+    if args.points:
+        N_POINTS = int(args.points)
+        WORKLOAD = WORKLOAD.replace("1M-point", f"{N_POINTS:,}-point")
     if args.workload == "features" and args.impl == "ours":
         if rank == 0:
             print(json.dumps(run_features(args)), flush=True)

@@ -51,6 +51,7 @@ struct FeatArgs {
     const SPoint<float>* row_map;  // optional: row r's output row is row_map[r].idx
     uint32_t uniform_k;            // ptr == nullptr: row r is nn[r * uniform_k, (r + 1) * uniform_k)
     uint32_t row_base;             // this launch covers rows [row_base, row_base + n_points)
+    int row_map_input;             // with row_map: row r also reads CSR row row_map[r].idx
 };
 
 struct RowCloud {
@@ -104,9 +105,10 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
     unsigned n_resolved = 0;
     if (i < a.row_base + a.n_points) {
         uint64_t b, e;
+        const uint32_t ri = a.row_map_input ? a.row_map[i].idx : i;
         if (a.ptr) {
-            b = __ldg(a.ptr + i);
-            e = __ldg(a.ptr + i + 1);
+            b = __ldg(a.ptr + ri);
+            e = __ldg(a.ptr + ri + 1);
         } else {
             b = (uint64_t)i * a.uniform_k;
             e = b + a.uniform_k;
@@ -282,6 +284,25 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
             const int r = t / row_w, c = t - r * row_w;
             a.out[(uint64_t)(row0 + r) * out_w + a.scale_offset * 11 + c] = stage[c * kFeatThreads + r];
         }
+    }
+}
+
+// Coordinates of each CSR row's first neighbour (point 0's for an empty or
+// invalid row): the key by which rows are ordered in space.
+__global__ void first_nb_kernel(const float* __restrict__ xyz, uint64_t n_xyz, const uint32_t* __restrict__ nn,
+                                uint64_t nnz, const uint32_t* __restrict__ ptr, uint64_t n_rows,
+                                float* __restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_rows;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = ptr[i], e = ptr[i + 1];
+        uint64_t id = 0;
+        if (e > b && b < nnz) {
+            id = nn[b];
+            if (id >= n_xyz) id = 0;
+        }
+        out[3 * i] = xyz[3 * id];
+        out[3 * i + 1] = xyz[3 * id + 1];
+        out[3 * i + 2] = xyz[3 * id + 2];
     }
 }
 
@@ -564,10 +585,12 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off,
-                    int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k, uint64_t row_base) {
+                    int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k, uint64_t row_base,
+                    bool row_map_input) {
     if (n_points == 0) return PGEOF_OK;
     FeatArgs a{};
     a.row_map = row_map;
+    a.row_map_input = row_map && row_map_input ? 1 : 0;
     a.uniform_k = uniform_k;
     a.row_base = (uint32_t)row_base;
     a.cloud_off = cloud_off;
@@ -607,6 +630,18 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
         if (st != PGEOF_OK) return st;
     }
     return PGEOF_OK;
+}
+
+int first_neighbour_xyz(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                        uint64_t n_rows, float* out, cudaStream_t s) {
+    if (n_rows == 0) return PGEOF_OK;
+    const DeviceInfo* di;
+    PGEOF_TRY(current_device_info(&di));
+    KernelTimer kt("row_order_kernels", s);
+    first_nb_kernel<<<std::min<unsigned>(ceil_div_u(n_rows, 256), (unsigned)di->sm_count * 8), 256, 0, s>>>(
+        xyz, n_xyz, nn, nnz, ptr, n_rows, out);
+    count_launch();
+    return check_launch("first_nb_kernel");
 }
 
 int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,

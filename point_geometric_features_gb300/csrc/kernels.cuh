@@ -13,13 +13,19 @@ int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s);
 // ptr == nullptr: every row has uniform_k neighbours (row i at nn[i * uniform_k]).
 // row_map (n_points entries): row i's features go to output row row_map[i].idx.
 // row_base: the launch covers rows [row_base, row_base + n_points) of ptr / out.
+// row_map_input: row i also reads CSR row row_map[i].idx (rows processed in the
+// order of row_map, each written to its own output row).
 template <typename T>
 struct SPoint;
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off = nullptr,
                     int n_clouds = 0, const SPoint<float>* row_map = nullptr, uint32_t uniform_k = 0,
-                    uint64_t row_base = 0);
+                    uint64_t row_base = 0, bool row_map_input = false);
+// out[3 i .. 3 i + 2]: coordinates of CSR row i's first neighbour (point 0's for
+// an empty or invalid row).
+int first_neighbour_xyz(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                        uint64_t n_rows, float* out, cudaStream_t s);
 int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                    uint64_t n_points, uint32_t k_min, uint32_t k_step, uint32_t k_min_search, float* out,
                    unsigned long long* stats, cudaStream_t s);

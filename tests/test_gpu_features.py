@@ -9,6 +9,8 @@ are compared after sign alignment where the reference's z-flip is undefined
 (|n_z| < 1e-4).
 """
 
+import os
+
 import numpy as np
 import pytest
 
@@ -249,3 +251,21 @@ def test_host_pipeline_large_csr_matches_device_path(cuda, pgeof):
     bad[n // 2] = bad[n // 2 + 1] + 7  # a decreasing step in the middle chunk
     with pytest.raises(ValueError):
         pgeof.compute_features(xyz, nn_h, bad)
+
+
+def test_row_order_is_invisible(cuda, tmp_path):
+    """Large clouds process CSR rows in the spatial order of their first
+    neighbour; forcing that on a small cloud (threshold 1 point) must give
+    the same bits as the plain order (threshold 0)."""
+    import subprocess
+    import sys
+
+    child = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_row_order_child.py")
+    outs = {}
+    for thr in ("0", "1"):
+        path = str(tmp_path / f"rows_{thr}.npz")
+        env = dict(os.environ, PGEOF_ROW_ORDER_POINTS=thr)
+        subprocess.run([sys.executable, child, path], env=env, check=True, timeout=300)
+        outs[thr] = np.load(path)
+    for key in ("f1", "f3", "g"):
+        np.testing.assert_array_equal(outs["0"][key], outs["1"][key])
