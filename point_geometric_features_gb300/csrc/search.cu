@@ -17,10 +17,12 @@
 //    buffer; selection then runs in shared memory (64-bin distance histogram,
 //    counting-sort scatter of the bins up to the k-th, insertion sort inside the
 //    few-entry bins). For kNN, tau comes from the queries the warp solved last
-//    (one per lane) by the triangle inequality, d_k(q) <= d_k(p) + |q - p|,
-//    minimised over the lanes, so only the first query of a chunk needs a pilot
-//    pass; radius search uses tau = r. A query whose buffer
-//    overflows goes to a list for the general kernel.
+//    (one per lane): d_k(p) + |q - p| / 2 minimised over the lanes, an
+//    optimistic form of the triangle inequality d_k(q) <= d_k(p) + |q - p| that
+//    is exact whenever it holds >= k points; only the first query of a chunk
+//    needs a pilot pass; radius search uses tau = r. Queries whose buffer
+//    overflows or whose radius fell short go to a list: a second fast pass with
+//    pilot bounds, then the general kernel.
 //  * search_kernel (float and double, any k): the general path. A pilot pass
 //    histograms a block of cells holding >= k points to bound the k-th distance,
 //    then passes over the cells within that bound refine a window of bins (first
@@ -734,12 +736,16 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
             bool strict;
             if (a.mode == MODE_KNN) {
                 strict = false;
-                // d_k(q) <= d_k(p) + |q - p| for every solved p: take the best over the lanes
+                // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
+                // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
+                // neighbours within 0.9 d_k(p)): when it holds >= k points the k
+                // nearest are all among them, otherwise (count < k) the query goes
+                // to the list pass, which re-solves it with a pilot bound.
                 float bound = INFINITY;
                 if (!LIST && rdk >= 0.0f && rci == ci) {
                     const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
                     const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (dq <= 0.75f * rdk) bound = rdk + dq;
+                    if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
                 }
                 bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
                 if (bound < INFINITY) {
@@ -773,7 +779,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
                                  count += __popc(mask);
                              });
             __syncwarp();
-            const bool short_knn = a.mode == MODE_KNN && count < k;  // rounding corner: never expected
+            const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
             const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
             const bool ok = count <= a.cap && !short_knn &&
                             (n_sel == 0 || select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, true));
