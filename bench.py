@@ -61,10 +61,11 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
-    p.add_argument("--workload", choices=["scene", "features", "batch", "serve", "optimal"], default="scene",
+    p.add_argument("--workload", choices=["scene", "features", "batch", "serve", "optimal", "index"], default="scene",
                    help="scene: the headline 1M-point kNN+multiscale step; features: the 1M-point k=50 "
                         "compute_features pass alone; batch: 256 clouds, plain vs batched; serve: Poisson request "
-                        "stream with p50/p99 latency; optimal: 4M-point radius -> optimal-k")
+                        "stream with p50/p99 latency; optimal: 4M-point radius -> optimal-k; index: searches on one "
+                        "resident grid vs per-call grids")
     p.add_argument("--points", type=int, default=None,
                    help="scene / features: cloud size (default 1,000,000; e.g. 4M and 16M for the asymptote)")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
@@ -612,6 +613,61 @@ def run_features(args):
     }
 
 
+def run_index(args):
+    """Resident index reuse on the 1M-point outdoor scene: one step = kNN at
+    k = 10, 20, 50 and a radius search (r = 0.5, max_knn = 64) over the whole
+    cloud, once through a GridIndex built before the timed region and once
+    through the per-call functions (one grid build per call, the reference's
+    pattern). Inputs (4M floats) and outputs stay on the device; the outputs
+    (1 GB per step) are larger than L2."""
+    import torch
+
+    import point_geometric_features_gb300 as pgeof
+    from point_geometric_features_gb300.synthetic import outdoor_scene
+
+    torch.cuda.set_device(0)
+    t = torch.from_numpy(outdoor_scene(N_POINTS, seed=1)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ix = pgeof.GridIndex(t, k_hint=K)
+    build_ms = (time.perf_counter() - t0) * 1e3
+
+    def step_index():
+        outs = [ix.knn_search(None, k) for k in (10, 20, 50)]
+        outs.append(ix.radius_search(None, 0.5, 64))
+        return outs
+
+    def step_call():
+        outs = [pgeof.knn_search(t, t, k) for k in (10, 20, 50)]
+        outs.append(pgeof.radius_search(t, t, 0.5, 64))
+        return outs
+
+    res = {}
+    for name, fn in (("index", step_index), ("per_call", step_call)):
+        for _ in range(max(args.warmup, 3)):
+            outs = fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            outs = fn()
+        b.record()
+        torch.cuda.synchronize()
+        res[name] = (a.elapsed_time(b) / args.steps, outs)
+    for (ai, ad), (bi, bd) in zip(res["index"][1], res["per_call"][1]):
+        assert torch.equal(ai.view(torch.int32), bi.view(torch.int32)) and torch.equal(ad, bd)
+    ix.close()
+    ms_ix, ms_call = res["index"][0], res["per_call"][0]
+    return {
+        "metric": "points/s resident-index searches (kNN k=10,20,50 + radius 0.5/64), 1M pts", "workload": "index",
+        "value": round(N_POINTS / ms_ix * 1e3, 1), "unit": UNIT, "ms_per_step": round(ms_ix, 4),
+        "per_call_ms_per_step": round(ms_call, 4), "index_build_ms": round(build_ms, 3), "steps": args.steps,
+        "dtype": "f32", "results_equal": True,
+        "config": {"workload": "1M-point outdoor scene, 3 kNN + 1 radius search per step on one resident grid",
+                   "points": N_POINTS, "k_hint": K, "l2": "outputs (1 GB per step) larger than L2"},
+    }
+
+
 def main():
     global N_POINTS, WORKLOAD
     args = parse()
@@ -630,6 +686,10 @@ def main():
     if args.workload == "serve" and args.impl == "ours":
         if rank == 0:
             print(json.dumps(run_serve(args)), flush=True)
+        return
+    if args.workload == "index" and args.impl == "ours":
+        if rank == 0:
+            print(json.dumps(run_index(args)), flush=True)
         return
     if args.workload == "batch" and args.impl == "ours":
         if rank == 0:

@@ -226,6 +226,39 @@ int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_
 int pgeof_batch_plan_launch(pgeof_batch_plan plan, pgeof_stream_t stream);
 int pgeof_batch_plan_destroy(pgeof_batch_plan plan);
 
+/* ------------------------------------------------ resident cloud index */
+/* The reference rebuilds its KD-tree inside every search call
+ * (include/nn_search.hpp:35,39,90,97; include/pgeof.hpp:330,333); a resident
+ * index builds one cloud's grid once and serves any number of searches with
+ * any k or radius, each returning exactly what pgeof_knn_search_f32 /
+ * pgeof_radius_search_f32 return for the same data (the search is exact for
+ * any cell size; the hints only steer its speed).
+ *
+ * create: `data` (device, (n_data, 3)) is read during the call only (the index
+ * keeps its own cell-ordered copy); k_hint = the neighbour count searches will
+ * mostly ask for (0: 16), radius_hint = their radius (0: none). Synchronises
+ * `stream`; afterwards any stream of the same device may search the index,
+ * concurrently. destroy waits for the searches enqueued so far.
+ * query == NULL searches the indexed points themselves (n_query ignored,
+ * n_data rows in the cloud's original order): the self-search of
+ * knn_search(xyz, xyz, k).
+ * index_knn_features: the kNN -> compute_features(k_min = 1) or
+ * compute_features_multiscale(k_scales) pipeline of pgeof_knn_features_f32
+ * on the indexed cloud; features (n_data, max(1, n_scales), 11). */
+typedef struct pgeof_index_s* pgeof_index;
+int pgeof_index_create_f32(const float* data, int64_t n_data, uint32_t k_hint, float radius_hint,
+                           pgeof_stream_t stream, pgeof_index* out);
+int pgeof_index_destroy(pgeof_index index);
+int pgeof_index_size(pgeof_index index, int64_t* n_points);
+/* nanoflann_knn_search<float>, include/nn_search.hpp:31-67, on the index. */
+int pgeof_index_knn_search_f32(pgeof_index index, const float* query, int64_t n_query, uint32_t knn,
+                               uint32_t* indices, float* sqr_dist, pgeof_stream_t stream);
+/* nanoflann_radius_search<float>, include/nn_search.hpp:85-132, on the index. */
+int pgeof_index_radius_search_f32(pgeof_index index, const float* query, int64_t n_query, float search_radius,
+                                  uint32_t max_knn, int32_t* indices, float* sqr_dist, pgeof_stream_t stream);
+int pgeof_index_knn_features_f32(pgeof_index index, uint32_t knn, const uint32_t* k_scales, int64_t n_scales,
+                                 float* features, pgeof_stream_t stream);
+
 /* ------------------------------------------------ host-pointer API (sync) */
 /* Same semantics as the device entry points above; every pointer is host
  * memory. These are what the Python drop-in binding calls for numpy inputs. */

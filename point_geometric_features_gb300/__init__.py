@@ -49,6 +49,7 @@ __all__ = [
     "check_device_errors",
     "batch_knn_features",
     "BatchPlan",
+    "GridIndex",
 ]
 
 
@@ -372,6 +373,139 @@ class BatchPlan:
         if getattr(self, "_h", 0):
             _ext._batch_plan_destroy(self._h)
             self._h = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------- resident index
+class GridIndex:
+    """One cloud's grid index built once and searched many times.
+
+    pgeof rebuilds its KD-tree inside every knn_search / radius_search call
+    (include/nn_search.hpp:35,39,90,97); ``GridIndex(data)`` builds the GPU
+    grid once, then ``knn_search``, ``radius_search`` and ``knn_features``
+    take any k or radius and return exactly what the module-level functions
+    return for the same data. ``query=None`` searches the indexed points
+    themselves (rows in the cloud's order). ``k_hint`` / ``radius_hint`` steer
+    the cell size towards the searches that will be asked for most (speed
+    only). ``data`` is a float32 (n, 3) numpy array (results come back as
+    numpy) or CUDA tensor (results stay on the device, enqueued on the current
+    torch stream); the index keeps its own copy of the points.
+    """
+
+    def __init__(self, data, k_hint=16, radius_hint=0.0):
+        import torch
+
+        self._numpy = not _is_torch(data)
+        if self._numpy:
+            import numpy as np
+
+            if not (isinstance(data, np.ndarray) and data.dtype == np.float32):
+                raise TypeError("GridIndex expects a float32 numpy array or a float32 CUDA tensor")
+            data = torch.from_numpy(np.ascontiguousarray(data)).cuda()
+        _dev_cloud(data, "data")
+        self.device = data.device
+        self.n = int(data.shape[0])
+        self._h = 0
+        with torch.cuda.device(self.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            self._h = _ext._index_create(data.data_ptr(), self.n, int(k_hint), float(radius_hint), s)
+
+    def __len__(self):
+        return self.n
+
+    def _query(self, torch, query):
+        if query is None:
+            return None, 0, self.n
+        if self._numpy != (not _is_torch(query)):
+            raise TypeError("query must be of the same kind (numpy or CUDA tensor) as the indexed data")
+        if self._numpy:
+            import numpy as np
+
+            if not (isinstance(query, np.ndarray) and query.dtype == np.float32):
+                raise TypeError("query must be a float32 numpy array")
+            query = torch.from_numpy(np.ascontiguousarray(query)).to(self.device)
+        _dev_cloud(query, "query")
+        if query.shape[0] == 0:  # (a NULL query pointer would mean the indexed points)
+            return query, None, 0
+        return query, query.data_ptr(), int(query.shape[0])
+
+    def _out(self, *ts, uint32_first=False):
+        """Results as given (CUDA tensors) or as numpy arrays for numpy inputs."""
+        if not self._numpy:
+            return ts if len(ts) > 1 else ts[0]
+        torch = _sys.modules["torch"]
+        res = [ts[0].view(torch.int32).cpu().numpy().view("uint32") if uint32_first else ts[0].cpu().numpy()]
+        res += [t.cpu().numpy() for t in ts[1:]]
+        return tuple(res) if len(res) > 1 else res[0]
+
+    def knn_search(self, query, knn):
+        """include/nn_search.hpp:31-67 on the index: (uint32 indices, float32 squared distances)."""
+        import torch
+
+        self._check_open()
+        q, qp, m = self._query(torch, query)
+        with torch.cuda.device(self.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            idx = _uint32_empty(torch, (m, int(knn)), self.device)
+            d2 = torch.empty((m, int(knn)), dtype=torch.float32, device=self.device)
+            if qp is None and int(knn) > self.n:
+                raise ValueError("knn size is greater than the data point cloud size")
+            if qp is not None:
+                _ext._dev_index_knn_search(self._h, qp, m if qp else 0, int(knn), idx.data_ptr(), d2.data_ptr(),
+                                           s)
+        del q
+        return self._out(idx, d2, uint32_first=True)
+
+    def radius_search(self, query, search_radius, max_knn):
+        """include/nn_search.hpp:85-132 on the index: (int32 indices, -1 = none; float32 squared distances)."""
+        import torch
+
+        self._check_open()
+        q, qp, m = self._query(torch, query)
+        with torch.cuda.device(self.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            idx = torch.empty((m, int(max_knn)), dtype=torch.int32, device=self.device)
+            d2 = torch.empty((m, int(max_knn)), dtype=torch.float32, device=self.device)
+            if qp is None and int(max_knn) > self.n:
+                raise ValueError("max knn size is greater than the data point cloud size")
+            if qp is not None:
+                _ext._dev_index_radius_search(self._h, qp, m if qp else 0, float(search_radius), int(max_knn),
+                                              idx.data_ptr(), d2.data_ptr(), s)
+        del q
+        return self._out(idx, d2)
+
+    def knn_features(self, k, k_scales=None):
+        """``knn_features(data, k, k_scales)`` on the indexed cloud."""
+        import torch
+
+        self._check_open()
+        scales = [int(v) for v in k_scales] if k_scales is not None else []
+        shape = (self.n, len(scales), 11) if scales else (self.n, 11)
+        with torch.cuda.device(self.device):
+            s = int(torch.cuda.current_stream().cuda_stream)
+            out = torch.zeros(shape, dtype=torch.float32, device=self.device)
+            _ext._dev_index_knn_features(self._h, int(k), scales, out.data_ptr(), s)
+        return self._out(out)
+
+    def _check_open(self):
+        if not self._h:
+            raise ValueError("the index is closed")
+
+    def close(self):
+        if getattr(self, "_h", 0):
+            _ext._index_destroy(self._h)
+            self._h = 0
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

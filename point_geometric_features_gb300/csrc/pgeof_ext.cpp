@@ -369,6 +369,38 @@ PYBIND11_MODULE(pgeof_ext, m) {
     m.def("_batch_plan_destroy", [](uintptr_t plan) {
         check(pgeof_batch_plan_destroy(reinterpret_cast<pgeof_batch_plan>(plan)));
     });
+    m.def("_index_create", [](uintptr_t data, int64_t n, uint32_t k_hint, float radius_hint, uintptr_t stream) {
+        pgeof_index ix = nullptr;
+        int st;
+        {
+            py::gil_scoped_release nogil;
+            st = pgeof_index_create_f32(P<const float>(data), n, k_hint, radius_hint, P<void>(stream), &ix);
+        }
+        check(st);
+        return reinterpret_cast<uintptr_t>(ix);
+    });
+    m.def("_index_destroy", [](uintptr_t ix) {
+        py::gil_scoped_release nogil;
+        check(pgeof_index_destroy(reinterpret_cast<pgeof_index>(ix)));
+    });
+    m.def("_dev_index_knn_search", [](uintptr_t ix, uintptr_t query, int64_t m_, uint32_t k, uintptr_t idx,
+                                      uintptr_t d2, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_index_knn_search_f32(reinterpret_cast<pgeof_index>(ix), P<const float>(query), m_, k,
+                                         P<uint32_t>(idx), P<float>(d2), P<void>(stream)));
+    });
+    m.def("_dev_index_radius_search", [](uintptr_t ix, uintptr_t query, int64_t m_, float r, uint32_t k,
+                                         uintptr_t idx, uintptr_t d2, uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_index_radius_search_f32(reinterpret_cast<pgeof_index>(ix), P<const float>(query), m_, r, k,
+                                            P<int32_t>(idx), P<float>(d2), P<void>(stream)));
+    });
+    m.def("_dev_index_knn_features", [](uintptr_t ix, uint32_t knn, std::vector<uint32_t> scales, uintptr_t out,
+                                        uintptr_t stream) {
+        py::gil_scoped_release nogil;
+        check(pgeof_index_knn_features_f32(reinterpret_cast<pgeof_index>(ix), knn, scales.data(),
+                                           (int64_t)scales.size(), P<float>(out), P<void>(stream)));
+    });
     m.def("_dev_compute_features_selected",
           [](uintptr_t xyz, int64_t n, double r, uint32_t max_knn, const std::vector<int32_t>& ids, bool f64,
              uintptr_t out, uintptr_t stream) {

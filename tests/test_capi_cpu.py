@@ -82,3 +82,25 @@ def test_eig_order_switch(pgeof):
     pgeof.set_eig_order("ascending")
     with pytest.raises(KeyError):
         pgeof.set_eig_order("sideways")
+
+
+def test_index_handle_argument_checks_without_device(pgeof):
+    """pgeof_index_*: argument errors come back before any device work."""
+    lib = ctypes.CDLL(pgeof.LIBRARY_PATH)
+    h = ctypes.c_void_p(0)
+    xyz = np.zeros((4, 3), np.float32)
+    ptr = xyz.ctypes.data_as(ctypes.c_void_p)
+    assert lib.pgeof_index_create_f32(ptr, ctypes.c_int64(0), 16, ctypes.c_float(0.0), None, ctypes.byref(h)) == 1
+    assert h.value is None
+    assert lib.pgeof_index_create_f32(ptr, ctypes.c_int64(4), 16, ctypes.c_float(-1.0), None, ctypes.byref(h)) == 1
+    assert lib.pgeof_index_create_f32(None, ctypes.c_int64(4), 16, ctypes.c_float(0.0), None, ctypes.byref(h)) == 1
+    assert lib.pgeof_index_create_f32(ptr, ctypes.c_int64(4), 16, ctypes.c_float(0.0), None, None) == 1
+    n = ctypes.c_int64(-1)
+    assert lib.pgeof_index_size(None, ctypes.byref(n)) == 1
+    assert lib.pgeof_index_knn_search_f32(None, None, ctypes.c_int64(0), 3, None, None, None) == 1
+    assert lib.pgeof_index_radius_search_f32(None, None, ctypes.c_int64(0), ctypes.c_float(0.1), 3, None, None,
+                                             None) == 1
+    assert lib.pgeof_index_knn_features_f32(None, 3, None, ctypes.c_int64(0), None, None) == 1
+    assert lib.pgeof_index_destroy(None) == 0
+    lib.pgeof_last_error_message.restype = ctypes.c_char_p
+    assert b"invalid index" in lib.pgeof_last_error_message()
