@@ -597,6 +597,19 @@ def run_features(args):
     assert out.shape == (N_POINTS, 11) and bool(torch.isfinite(out).all())
     ms = sum(a.elapsed_time(b) for a, b in zip(starts, stops)) / args.steps
     n, kms = prof.get("features_kernel", (args.steps, ms * args.steps))
+    # the float64 instantiation of the same pass (precision path, FP64-bound)
+    t64 = t.double()
+    for _ in range(2):
+        out64 = pgeof.compute_features(t64, nn, ptr, check=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        out64 = pgeof.compute_features(t64, nn, ptr, check=False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / args.steps
+    f64_dev = float(((out64 - out.double()).abs() / out64.abs().clamp(min=1.0)).max())
     per_launch_ms = kms / n
     algo = 4 * K + 4 + 12 + 44
     peak, peak_kind = measured_peaks()
@@ -610,6 +623,9 @@ def run_features(args):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": algo * N_POINTS, "avg_launch_ms": round(per_launch_ms, 4),
                      "traffic": traffic_from_profile("features_kernel")},
+        "f64": {"ms_per_step": round(ms64, 4), "value": round(N_POINTS / ms64 * 1e3, 1), "unit": UNIT,
+                "max_scaled_diff_vs_f32": f64_dev,
+                "path": "compute_features on a float64 CUDA tensor (real_t = double instantiation)"},
     }
 
 

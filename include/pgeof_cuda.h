@@ -171,6 +171,22 @@ int pgeof_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const ui
                                        const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
                                        uint32_t k_min_search, float* features, pgeof_stream_t stream);
 
+/* The three CSR feature passes above for a float64 cloud: the reference's
+ * drivers and PCA are templates on real_t (include/pgeof.hpp:75-117, 123-211,
+ * 243-310; include/pca.hpp:72-200) that its binding instantiates for float
+ * only; these are the real_t = double instantiations (two-pass covariance,
+ * eigen solve and feature formulas in double). Same arguments, checks, zero
+ * rules and output layouts, with double xyz and double features. */
+int pgeof_compute_features_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                               const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, double* features,
+                               pgeof_stream_t stream);
+int pgeof_compute_features_multiscale_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                          const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                          int64_t n_scales, double* features, pgeof_stream_t stream);
+int pgeof_compute_features_optimal_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                       const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
+                                       uint32_t k_min_search, double* features, pgeof_stream_t stream);
+
 /* compute_geometric_features_selected<float>, include/pgeof.hpp:325-375.
  * Radius search (< search_radius^2) around every point, the nearest max_knn
  * kept, PCA, then the selected EFeatureIDs in list order. `selected` is a HOST
@@ -280,6 +296,15 @@ int pgeof_host_compute_features_multiscale_f32(const float* xyz, int64_t n_xyz, 
 int pgeof_host_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
                                             const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min,
                                             uint32_t k_step, uint32_t k_min_search, float* features);
+/* float64 instantiations of the three passes above */
+int pgeof_host_compute_features_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                    const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, double* features);
+int pgeof_host_compute_features_multiscale_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                               const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                               int64_t n_scales, double* features);
+int pgeof_host_compute_features_optimal_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                            const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min,
+                                            uint32_t k_step, uint32_t k_min_search, double* features);
 /* include/pgeof.hpp:325-375 (float) */
 int pgeof_host_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
                                              const int32_t* selected, int64_t n_selected, float* features);

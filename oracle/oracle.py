@@ -74,6 +74,7 @@ def _load():
             lib.oracle_radius_search.argtypes = [P, S, P, S, ctypes.c_float, U, I, P, P]
             lib.oracle_selected_f32.argtypes = [P, S, ctypes.c_float, U, P, S, I, I, P]
             lib.oracle_selected_f64.argtypes = [P, S, ctypes.c_double, U, P, S, I, I, P]
+            lib.oracle_compute_features_f64.argtypes = [I, P, P, P, S, S, P, S, U, U, I, I, P]
             lib.oracle_pca_features_f32.argtypes = [P, S, I, P]
             lib.oracle_pca_features_f32.restype = None
             lib.oracle_covariance_f32.argtypes = [P, S, P]
@@ -82,7 +83,7 @@ def _load():
             for f in (
                 lib.oracle_compute_features, lib.oracle_compute_features_multiscale,
                 lib.oracle_compute_features_optimal, lib.oracle_knn_search, lib.oracle_radius_search,
-                lib.oracle_selected_f32, lib.oracle_selected_f64,
+                lib.oracle_selected_f32, lib.oracle_selected_f64, lib.oracle_compute_features_f64,
             ):
                 f.restype = I
             _lib = lib
@@ -139,6 +140,24 @@ def compute_features_optimal(xyz, nn, nn_ptr, k_min=1, k_step=1, k_min_search=1,
         _ptr(xyz), _ptr(nn), _ptr(nn_ptr), n, int(k_min), int(k_step), int(k_min_search), order, threads, _ptr(out)
     ):
         raise ValueError("k_min and k_min_search should be > 1 (and k_step >= 1)")
+    return out
+
+
+def compute_features_f64(xyz, nn, nn_ptr, k_min=1, kind="full", k_scales=(), k_step=1, k_min_search=1,
+                         order=EIG_ASCENDING, threads=0):
+    """include/pgeof.hpp:75-117 / 123-211 / 243-310 (kind "full" / "multi" /
+    "optimal") with real_t = double: the same drivers and PCA in double."""
+    lib = _load()
+    xyz, nn, nn_ptr = _c(xyz, np.float64), _c(nn, np.uint32), _c(nn_ptr, np.uint32)
+    scales = _c(np.asarray(k_scales if kind == "multi" else [1]), np.uint32)
+    n = nn_ptr.size - 1
+    code = {"full": 0, "multi": 1, "optimal": 2}[kind]
+    shape = {"full": (n, 11), "multi": (n, scales.size, 11), "optimal": (n, 12)}[kind]
+    out = np.zeros(shape, np.float64)
+    if lib.oracle_compute_features_f64(code, _ptr(xyz), _ptr(nn), _ptr(nn_ptr), n, int(k_min), _ptr(scales),
+                                       scales.size if kind == "multi" else 0, int(k_step), int(k_min_search), order,
+                                       threads, _ptr(out)):
+        raise ValueError("invalid k_min / k_scales / k_step")
     return out
 
 

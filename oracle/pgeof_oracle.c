@@ -334,6 +334,109 @@ int oracle_compute_features_optimal(const float* xyz, const uint32_t* nn, const 
 }
 
 /* ------------------------------------------------------------------------- */
+/* the same three drivers with real_t = double (the templates of              */
+/* include/pgeof.hpp instantiated for double; pgeof binds them for float only) */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    const double* xyz;
+    const uint32_t* nn;
+    const uint32_t* ptr;
+    size_t k_min;
+    int order;
+    double* out;
+    const uint32_t* scales;
+    size_t n_scales;
+    uint32_t k_step, k_min_search;
+    int kind;
+} csr64_ctx;
+
+static double* gather_f64(const double* xyz, const uint32_t* nn, size_t base, size_t k) {
+    double* pts = (double*)malloc(sizeof(double) * 3 * (k ? k : 1));
+    for (size_t j = 0; j < k; ++j) {
+        const size_t id = nn[base + j];
+        pts[3 * j + 0] = xyz[3 * id + 0];
+        pts[3 * j + 1] = xyz[3 * id + 1];
+        pts[3 * j + 2] = xyz[3 * id + 2];
+    }
+    return pts;
+}
+
+/* include/pgeof.hpp:93-109, 183-199, 264-299 for double */
+static void range_f64(void* vctx, size_t lo, size_t hi) {
+    csr64_ctx* c = (csr64_ctx*)vctx;
+    for (size_t i = lo; i < hi; ++i) {
+        const size_t k_nn = (size_t)(uint32_t)(c->ptr[i + 1] - c->ptr[i]);
+        if (c->kind == 0) {
+            if (k_nn < c->k_min) continue;
+            double* pts = gather_f64(c->xyz, c->nn, c->ptr[i], k_nn);
+            pca_f64 p;
+            pca_from_pointcloud_f64(pts, k_nn, c->order, &p);
+            compute_features_f64(&p, &c->out[i * 11]);
+            free(pts);
+        } else if (c->kind == 1) {
+            for (size_t s = 0; s < c->n_scales; ++s) {
+                const size_t ks = c->scales[s];
+                if (k_nn < ks) break;
+                double* pts = gather_f64(c->xyz, c->nn, c->ptr[i], ks);
+                pca_f64 p;
+                pca_from_pointcloud_f64(pts, ks, c->order, &p);
+                compute_features_f64(&p, &c->out[(i * c->n_scales + s) * 11]);
+                free(pts);
+            }
+        } else {
+            const size_t kmin = c->k_min, kms = c->k_min_search;
+            if (!(k_nn >= kmin && k_nn >= kms)) continue;
+            size_t k0 = kmin > kms ? kmin : kms;
+            if (k0 > k_nn) k0 = k_nn;
+            double* pts = gather_f64(c->xyz, c->nn, c->ptr[i], k_nn);
+            pca_f64 best;
+            double best_e = 1.0;
+            size_t k_opt = k_nn;
+            for (size_t k = k0; k <= k_nn; ++k) {
+                if (k > k0 && (k % c->k_step) != 0 && k != k_nn) continue;
+                pca_f64 p;
+                pca_from_pointcloud_f64(pts, k, c->order, &p);
+                const double e = compute_eigentropy_f64(&p);
+                if (k == k0 || e < best_e) {
+                    best_e = e;
+                    k_opt = k;
+                    best = p;
+                }
+            }
+            compute_features_f64(&best, &c->out[i * 12]);
+            c->out[i * 12 + 11] = (double)k_opt;
+            free(pts);
+        }
+    }
+}
+
+/* kind 0: compute_features (out n x 11), 1: multiscale (n x n_scales x 11),
+ * 2: optimal (n x 12). Returns 1 on the reference's argument errors. */
+int oracle_compute_features_f64(int kind, const double* xyz, const uint32_t* nn, const uint32_t* ptr, size_t n,
+                                size_t k_min, const uint32_t* scales, size_t n_scales, uint32_t k_step,
+                                uint32_t k_min_search, int order, int nthreads, double* out) {
+    size_t width = 11;
+    if (kind == 0 && k_min < 1) return 1;
+    if (kind == 1) {
+        uint32_t prev = 1;
+        for (size_t s = 0; s < n_scales; ++s) {
+            if (scales[s] < prev) return 1;
+            prev = scales[s];
+        }
+        width = n_scales * 11;
+    }
+    if (kind == 2) {
+        if (k_min < 1 && k_min_search < 1) return 1;
+        if (k_step < 1) return 1;
+        width = 12;
+    }
+    memset(out, 0, sizeof(double) * n * width);
+    csr64_ctx c = {xyz, nn, ptr, k_min, order, out, scales, n_scales, k_step, k_min_search, kind};
+    parallel_for(n, nthreads, range_f64, &c);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
 /* neighbour search (include/nn_search.hpp with nanoflann semantics)          */
 /* ------------------------------------------------------------------------- */
 /* metric_L2_Simple: result = 0; result += (a_i - b_i)^2 for i = x, y, z. */

@@ -38,6 +38,9 @@ __all__ = [
     "compute_features",
     "compute_features_multiscale",
     "compute_features_optimal",
+    "compute_features_f64",
+    "compute_features_multiscale_f64",
+    "compute_features_optimal_f64",
     "knn_search",
     "radius_search",
     "radius_search_csr",
@@ -143,6 +146,8 @@ def _finish(check, stream):
 
 def _dev_features(kind, xyz, nn, nn_ptr, args, check):
     torch = _sys.modules["torch"]
+    if xyz.dtype == torch.float64:
+        return _dev_features_f64(kind, xyz, nn, nn_ptr, args, check)
     _dev_cloud(xyz, "xyz")
     _dev_index(nn, "nn")
     _dev_index(nn_ptr, "nn_ptr")
@@ -167,6 +172,27 @@ def _dev_features(kind, xyz, nn, nn_ptr, args, check):
     return out
 
 
+def _dev_features_f64(kind, xyz, nn, nn_ptr, args, check):
+    torch = _sys.modules["torch"]
+    _dev_cloud(xyz, "xyz", "float64")
+    _dev_index(nn, "nn")
+    _dev_index(nn_ptr, "nn_ptr")
+    n = max(nn_ptr.shape[0] - 1, 0)
+    code = {"full": 0, "multi": 1, "optimal": 2}[kind]
+    scales = [int(v) for v in args[0]] if kind == "multi" else []
+    k_min = int(args[0]) if kind != "multi" else 1
+    k_step, k_min_search = (int(args[1]), int(args[2])) if kind == "optimal" else (1, 1)
+    shape = {"full": (n, 11), "multi": (n, len(scales), 11), "optimal": (n, 12)}[kind]
+    with torch.cuda.device(xyz.device):
+        s = int(torch.cuda.current_stream().cuda_stream)
+        out = torch.zeros(shape, dtype=torch.float64, device=xyz.device)
+        _ext._dev_compute_features_f64(code, xyz.data_ptr(), xyz.shape[0], nn.data_ptr(), nn.shape[0],
+                                       nn_ptr.data_ptr(), nn_ptr.shape[0] - 1, k_min, scales, k_step, k_min_search,
+                                       out.data_ptr(), s)
+        _finish(check, s)
+    return out
+
+
 # --------------------------------------------------------------- public API
 def compute_features(xyz, nn, nn_ptr, k_min=1, verbose=False, *, check=True):
     """include/pgeof.hpp:75-117 -- (n_points, 11) float32 features from CSR neighbours."""
@@ -187,6 +213,31 @@ def compute_features_optimal(xyz, nn, nn_ptr, k_min=1, k_step=1, k_min_search=1,
     if _is_torch(xyz):
         return _dev_features("optimal", xyz, nn, nn_ptr, (k_min, k_step, k_min_search), check)
     return _ext.compute_features_optimal(xyz, nn, nn_ptr, k_min, k_step, k_min_search, verbose)
+
+
+def compute_features_f64(xyz, nn, nn_ptr, k_min=1, verbose=False, *, check=True):
+    """compute_features for a float64 cloud (include/pgeof.hpp:75-117 with
+    real_t = double, which pgeof's binding does not instantiate): (n_points, 11)
+    float64. numpy arrays or CUDA tensors, as compute_features."""
+    if _is_torch(xyz):
+        return _dev_features_f64("full", xyz, nn, nn_ptr, (k_min,), check)
+    return _ext.compute_features_f64(xyz, nn, nn_ptr, k_min, verbose)
+
+
+def compute_features_multiscale_f64(xyz, nn, nn_ptr, k_scales, verbose=False, *, check=True):
+    """compute_features_multiscale for a float64 cloud (include/pgeof.hpp:123-211
+    with real_t = double): (n_points, n_scales, 11) float64."""
+    if _is_torch(xyz):
+        return _dev_features_f64("multi", xyz, nn, nn_ptr, (k_scales,), check)
+    return _ext.compute_features_multiscale_f64(xyz, nn, nn_ptr, k_scales, verbose)
+
+
+def compute_features_optimal_f64(xyz, nn, nn_ptr, k_min=1, k_step=1, k_min_search=1, verbose=False, *, check=True):
+    """compute_features_optimal for a float64 cloud (include/pgeof.hpp:243-310
+    with real_t = double): (n_points, 12) float64, column 11 = optimal k."""
+    if _is_torch(xyz):
+        return _dev_features_f64("optimal", xyz, nn, nn_ptr, (k_min, k_step, k_min_search), check)
+    return _ext.compute_features_optimal_f64(xyz, nn, nn_ptr, k_min, k_step, k_min_search, verbose)
 
 
 def knn_search(data, query, knn):

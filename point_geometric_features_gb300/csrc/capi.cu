@@ -695,6 +695,36 @@ int pgeof_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, const ui
                          features, (cudaStream_t)stream);
 }
 
+int pgeof_compute_features_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                               const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, double* features,
+                               pgeof_stream_t stream) {
+    if (k_min < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min should be > 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return launch_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 0, k_min, nullptr, 0, 0, 0, features,
+                               (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_multiscale_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                          const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                          int64_t n_scales, double* features, pgeof_stream_t stream) {
+    if (n_scales < 0 || n_scales > (1 << 20) || (n_scales > 0 && !k_scales) || !check_scales(k_scales, n_scales))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales should be > 1 and sorted in ascending order");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return launch_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 1, 1, k_scales, (int)n_scales, 0, 0,
+                               features, (cudaStream_t)stream);
+}
+
+int pgeof_compute_features_optimal_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                       const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min, uint32_t k_step,
+                                       uint32_t k_min_search, double* features, pgeof_stream_t stream) {
+    if (k_min < 1 && k_min_search < 1)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min and k_min_search should be > 1");
+    if (k_step < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_step should be >= 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return launch_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 2, k_min, nullptr, 0, k_step, k_min_search,
+                               features, (cudaStream_t)stream);
+}
+
 int pgeof_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,
                                         const int32_t* selected, int64_t n_selected, float* features,
                                         pgeof_stream_t stream) {
@@ -912,6 +942,56 @@ int pgeof_host_compute_features_optimal_f32(const float* xyz, int64_t n_xyz, con
     PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
     return host_features(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 2, k_min, nullptr, 0, k_step, k_min_search,
                          features, 12);
+}
+
+// Host-pointer float64 feature passes: upload, one kernel, download.
+static int host_features_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                             const uint32_t* nn_ptr, int64_t n_points, int kind, uint64_t k_min,
+                             const uint32_t* scales, int64_t n_scales, uint32_t k_step, uint32_t k_min_search,
+                             double* features, uint64_t row_width) {
+    if (n_points == 0 || row_width == 0) return PGEOF_OK;
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    Scratch d_xyz, d_nn, d_ptr, d_out;
+    PGEOF_TRY(upload(d_xyz, xyz, 3ull * n_xyz, s));
+    PGEOF_TRY(upload(d_nn, nn, (uint64_t)nnz, s));
+    PGEOF_TRY(upload(d_ptr, nn_ptr, (uint64_t)n_points + 1, s));
+    const uint64_t cnt = (uint64_t)n_points * row_width;
+    PGEOF_TRY(d_out.alloc(cnt * sizeof(double), s));
+    PGEOF_TRY(launch_features_f64(d_xyz.as<double>(), n_xyz, d_nn.as<uint32_t>(), nnz, d_ptr.as<uint32_t>(),
+                                  n_points, kind, k_min, scales, (int)n_scales, k_step, k_min_search,
+                                  d_out.as<double>(), s));
+    PGEOF_TRY(download(features, d_out, cnt, s));
+    return finish_host(ce, s);
+}
+
+int pgeof_host_compute_features_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                    const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, double* features) {
+    if (k_min < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min should be > 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 0, k_min, nullptr, 0, 0, 0, features, 11);
+}
+
+int pgeof_host_compute_features_multiscale_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                               const uint32_t* nn_ptr, int64_t n_points, const uint32_t* k_scales,
+                                               int64_t n_scales, double* features) {
+    if (n_scales < 0 || n_scales > (1 << 20) || (n_scales > 0 && !k_scales) || !check_scales(k_scales, n_scales))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_scales should be > 1 and sorted in ascending order");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 1, 1, k_scales, n_scales, 0, 0, features,
+                             (uint64_t)n_scales * 11);
+}
+
+int pgeof_host_compute_features_optimal_f64(const double* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
+                                            const uint32_t* nn_ptr, int64_t n_points, uint32_t k_min,
+                                            uint32_t k_step, uint32_t k_min_search, double* features) {
+    if (k_min < 1 && k_min_search < 1)
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_min and k_min_search should be > 1");
+    if (k_step < 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "k_step should be >= 1");
+    PGEOF_TRY(check_csr(n_xyz, nnz, n_points));
+    return host_features_f64(xyz, n_xyz, nn, nnz, nn_ptr, n_points, 2, k_min, nullptr, 0, k_step, k_min_search,
+                             features, 12);
 }
 
 int pgeof_host_compute_features_selected_f32(const float* xyz, int64_t n, float search_radius, uint32_t max_knn,

@@ -22,6 +22,12 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off = nullptr,
                     int n_clouds = 0, const SPoint<float>* row_map = nullptr, uint32_t uniform_k = 0,
                     uint64_t row_base = 0, bool row_map_input = false);
+// The three CSR feature passes for a float64 cloud (kind 0 compute_features,
+// 1 multiscale over the HOST array `scales`, 2 optimal); out is float64 with
+// rows of 11, n_scales * 11 or 12 values.
+int launch_features_f64(const double* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
+                        uint64_t n_points, int kind, uint64_t k_min, const uint32_t* scales, int n_scales,
+                        uint32_t k_step, uint32_t k_min_search, double* out, cudaStream_t s);
 // out[3 i .. 3 i + 2]: coordinates of CSR row i's first neighbour (point 0's for
 // an empty or invalid row).
 int first_neighbour_xyz(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,

@@ -146,6 +146,33 @@ f32arr compute_features_optimal(const f32arr& xyz, const u32arr& nn, const u32ar
     return out;
 }
 
+// float64 instantiations of the three CSR passes (kind 0 / 1 / 2)
+f64arr features_f64(int kind, const f64arr& xyz, const u32arr& nn, const u32arr& nn_ptr, uint64_t k_min,
+                    const std::vector<uint32_t>& k_scales, uint32_t k_step, uint32_t k_min_search, bool verbose) {
+    const int64_t n_xyz = cloud_rows(xyz, "xyz");
+    const int64_t nnz = vec_len(nn, "nn"), np1 = vec_len(nn_ptr, "nn_ptr");
+    const int64_t n = np1 - 1, rows = std::max<int64_t>(n, 0);
+    f64arr out = kind == 1 ? result_array<double>({rows, (int64_t)k_scales.size(), (int64_t)11})
+                           : result_array<double>({rows, (int64_t)(kind == 2 ? 12 : 11)});
+    int st;
+    {
+        py::gil_scoped_release nogil;
+        if (kind == 0)
+            st = pgeof_host_compute_features_f64(xyz.data(), n_xyz, nn.data(), nnz, nn_ptr.data(), n, k_min,
+                                                 out.mutable_data());
+        else if (kind == 1)
+            st = pgeof_host_compute_features_multiscale_f64(xyz.data(), n_xyz, nn.data(), nnz, nn_ptr.data(), n,
+                                                            k_scales.data(), (int64_t)k_scales.size(),
+                                                            out.mutable_data());
+        else
+            st = pgeof_host_compute_features_optimal_f64(xyz.data(), n_xyz, nn.data(), nnz, nn_ptr.data(), n,
+                                                         (uint32_t)k_min, k_step, k_min_search, out.mutable_data());
+    }
+    check(st);
+    progress_done(verbose, n);
+    return out;
+}
+
 std::pair<u32arr, f32arr> knn_search(const f32arr& data, const f32arr& query, uint32_t knn) {
     const int64_t n = cloud_rows(data, "data"), m = cloud_rows(query, "query");
     u32arr idx = result_array<uint32_t>({m, (int64_t)knn});
@@ -254,6 +281,28 @@ PYBIND11_MODULE(pgeof_ext, m) {
           py::arg("k_min_search") = 1, py::arg("verbose") = false,
           "Features at the neighbourhood size of minimal eigentropy (Weinmann et al. 2015).\n"
           "Returns a (n_points, 12) float32 array; column 11 is the optimal size.");
+    m.def(
+        "compute_features_f64",
+        [](const f64arr& xyz, const u32arr& nn, const u32arr& nn_ptr, uint64_t k_min, bool verbose) {
+            return features_f64(0, xyz, nn, nn_ptr, k_min, {}, 1, 1, verbose);
+        },
+        py::arg("xyz").noconvert(), py::arg("nn").noconvert(), py::arg("nn_ptr").noconvert(), py::arg("k_min") = 1,
+        py::arg("verbose") = false, "compute_features for a float64 cloud; (n_points, 11) float64.");
+    m.def(
+        "compute_features_multiscale_f64",
+        [](const f64arr& xyz, const u32arr& nn, const u32arr& nn_ptr, const std::vector<uint32_t>& k_scales,
+           bool verbose) { return features_f64(1, xyz, nn, nn_ptr, 1, k_scales, 1, 1, verbose); },
+        py::arg("xyz").noconvert(), py::arg("nn").noconvert(), py::arg("nn_ptr").noconvert(), py::arg("k_scales"),
+        py::arg("verbose") = false, "compute_features_multiscale for a float64 cloud; (n_points, n_scales, 11).");
+    m.def(
+        "compute_features_optimal_f64",
+        [](const f64arr& xyz, const u32arr& nn, const u32arr& nn_ptr, uint32_t k_min, uint32_t k_step,
+           uint32_t k_min_search, bool verbose) {
+            return features_f64(2, xyz, nn, nn_ptr, k_min, {}, k_step, k_min_search, verbose);
+        },
+        py::arg("xyz").noconvert(), py::arg("nn").noconvert(), py::arg("nn_ptr").noconvert(), py::arg("k_min") = 1,
+        py::arg("k_step") = 1, py::arg("k_min_search") = 1, py::arg("verbose") = false,
+        "compute_features_optimal for a float64 cloud; (n_points, 12) float64, column 11 the optimal size.");
     m.def("knn_search", &knn_search, py::arg("data").noconvert(), py::arg("query").noconvert(), py::arg("knn"),
           "For each query point, the knn nearest data points: (uint32 indices, float32 squared distances),\n"
           "both (n_query, knn), ascending.");
@@ -401,6 +450,24 @@ PYBIND11_MODULE(pgeof_ext, m) {
         check(pgeof_index_knn_features_f32(reinterpret_cast<pgeof_index>(ix), knn, scales.data(),
                                            (int64_t)scales.size(), P<float>(out), P<void>(stream)));
     });
+    m.def("_dev_compute_features_f64",
+          [](int kind, uintptr_t xyz, int64_t n_xyz, uintptr_t nn, int64_t nnz, uintptr_t ptr, int64_t n,
+             uint64_t k_min, const std::vector<uint32_t>& scales, uint32_t k_step, uint32_t k_min_search,
+             uintptr_t out, uintptr_t stream) {
+              py::gil_scoped_release nogil;
+              if (kind == 0)
+                  check(pgeof_compute_features_f64(P<const double>(xyz), n_xyz, P<const uint32_t>(nn), nnz,
+                                                   P<const uint32_t>(ptr), n, k_min, P<double>(out), P<void>(stream)));
+              else if (kind == 1)
+                  check(pgeof_compute_features_multiscale_f64(P<const double>(xyz), n_xyz, P<const uint32_t>(nn),
+                                                              nnz, P<const uint32_t>(ptr), n, scales.data(),
+                                                              (int64_t)scales.size(), P<double>(out),
+                                                              P<void>(stream)));
+              else
+                  check(pgeof_compute_features_optimal_f64(P<const double>(xyz), n_xyz, P<const uint32_t>(nn), nnz,
+                                                           P<const uint32_t>(ptr), n, (uint32_t)k_min, k_step,
+                                                           k_min_search, P<double>(out), P<void>(stream)));
+          });
     m.def("_dev_compute_features_selected",
           [](uintptr_t xyz, int64_t n, double r, uint32_t max_knn, const std::vector<int32_t>& ids, bool f64,
              uintptr_t out, uintptr_t stream) {

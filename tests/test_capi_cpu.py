@@ -104,3 +104,21 @@ def test_index_handle_argument_checks_without_device(pgeof):
     assert lib.pgeof_index_destroy(None) == 0
     lib.pgeof_last_error_message.restype = ctypes.c_char_p
     assert b"invalid index" in lib.pgeof_last_error_message()
+
+
+def test_f64_feature_argument_errors_without_device(pgeof):
+    xyz = np.random.default_rng(0).random((20, 3))
+    nn = np.arange(20, dtype=np.uint32)
+    ptr = np.array([0, 10, 20], np.uint32)
+    with pytest.raises(ValueError, match="k_min should be"):
+        pgeof.compute_features_f64(xyz, nn, ptr, 0)
+    with pytest.raises(ValueError, match="k_scales"):
+        pgeof.compute_features_multiscale_f64(xyz, nn, ptr, [10, 5])
+    with pytest.raises(ValueError, match="k_min and k_min_search"):
+        pgeof.compute_features_optimal_f64(xyz, nn, ptr, 0, 1, 0)
+    with pytest.raises(ValueError, match="k_step"):
+        pgeof.compute_features_optimal_f64(xyz, nn, ptr, 1, 0, 1)
+    with pytest.raises(TypeError):  # noconvert: float32 xyz is not cast
+        pgeof.compute_features_f64(xyz.astype(np.float32), nn, ptr)
+    with pytest.raises(TypeError):
+        pgeof.compute_features(xyz, nn, ptr)  # the reference's float32-only entry point stays strict

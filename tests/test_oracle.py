@@ -183,3 +183,34 @@ def test_selected_matches_features():
             assert np.all(sel[i] == 0)
             continue
         np.testing.assert_array_equal(sel[i], oracle.pca_features(xyz[row])["features"])
+
+
+def test_f64_oracle_vs_numpy_fp64(golden):
+    """The double-instantiation drivers (real_t = double) agree with the
+    independent numpy FP64 restatement (eigh) on the golden cloud, and their
+    multiscale / optimal drivers keep the float drivers' rules."""
+    g = golden("features_2000_k20.npz")
+    xyz, idx = g["xyz"].astype(np.float64), g["idx"]
+    n, k = idx.shape
+    nn = idx.reshape(-1).astype(np.uint32)
+    ptr = (np.arange(n + 1) * k).astype(np.uint32)
+    f = oracle.compute_features_f64(xyz, nn, ptr)
+    ref = g["features_fp64"]
+    gap = oracle.fp64_relative_gap(g["xyz"][idx])
+    ok = gap > 1e-6
+    err = np.abs(f - ref) / np.maximum(1.0, np.abs(ref))
+    assert err[ok].max() < 1e-9, err[ok].max()
+    assert np.abs(f[:, 7] - ref[:, 7]).max() < 1e-12  # Length: eigenvalue only
+    m = oracle.compute_features_f64(xyz, nn, ptr, kind="multi", k_scales=[5, 10, k])
+    np.testing.assert_array_equal(m[:, 2], f)
+    # ragged rows: scales the row cannot fill stay 0 and so do the later ones
+    nn_r = np.concatenate([nn[ptr[i]:ptr[i] + 7] for i in range(n)])
+    ptr_r = (np.arange(n + 1) * 7).astype(np.uint32)
+    m = oracle.compute_features_f64(xyz, nn_r, ptr_r, kind="multi", k_scales=[5, 10, 20])
+    assert np.all(m[:, 1:] == 0) and np.all(m[:, 0, 7] > 0)
+    o = oracle.compute_features_f64(xyz, nn, ptr, 1, kind="optimal", k_step=3, k_min_search=6)
+    o32 = oracle.compute_features_optimal(g["xyz"], nn, ptr, 1, 3, 6)
+    assert np.mean(o[:, 11] == o32[:, 11]) > 0.99
+    assert set(np.unique(o[:, 11])) <= {6, 9, 12, 15, 18, 20}
+    with pytest.raises(ValueError):
+        oracle.compute_features_f64(xyz, nn, ptr, 0)
