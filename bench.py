@@ -69,6 +69,8 @@ def parse():
     p.add_argument("--points", type=int, default=None,
                    help="scene / features: cloud size (default 1,000,000; e.g. 4M and 16M for the asymptote)")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    p.add_argument("--server", choices=["native", "python"], default="native",
+                   help="serve: the library's C++ request server or the Python one")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
     return p.parse_args()
 
@@ -489,14 +491,14 @@ def run_serve(args):
     bound the client, not the server)."""
     import torch
 
-    from point_geometric_features_gb300.serving import Server, run_stream
+    from point_geometric_features_gb300.serving import NativeServer, Server, run_stream
     from point_geometric_features_gb300.synthetic import log_uniform_sizes, scaled_scene
 
     torch.cuda.set_device(0)
     rng = np.random.default_rng(4)
     sizes = log_uniform_sizes(96, 1_000, 500_000, seed=4)
     pool = [scaled_scene(int(n), seed=4000 + i, side=float(rng.uniform(5.0, 50.0))) for i, n in enumerate(sizes)]
-    server = Server(slots=8, budget_bytes=40 << 30)
+    server = (NativeServer if args.server == "native" else Server)(slots=8, budget_bytes=40 << 30)
     try:
         run_stream(server, pool, rate=args.rate, duration=min(3.0, args.duration), seed=40)  # warm-up
         server.results.clear()
@@ -508,7 +510,9 @@ def run_serve(args):
         "workload": "serve",
         "config": {"rate_per_s": args.rate, "duration_s": args.duration, "sizes": "log-uniform [1000, 500000]",
                    "k": [16, 32, 64], "features": ["Verticality", "Curvature", "Planarity", "Normal_z"],
-                   "budget_bytes": 40 << 30, "slots": 8},
+                   "budget_bytes": 40 << 30, "slots": 8,
+                   "server": "library (pgeof_server_*, C++ workers)" if args.server == "native"
+                   else "Python (serving.Server, torch streams)"},
         "p50_ms": round(out["p50_ms"], 3),
         "p99_ms": round(out["p99_ms"], 3),
         "mean_ms": round(out["mean_ms"], 3),

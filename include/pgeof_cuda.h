@@ -242,6 +242,33 @@ int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_
 int pgeof_batch_plan_launch(pgeof_batch_plan plan, pgeof_stream_t stream);
 int pgeof_batch_plan_destroy(pgeof_batch_plan plan);
 
+/* ------------------------------------------------ request server */
+/* compute_features_selected (include/pgeof.hpp:325-375) served to a stream of
+ * independent requests (no reference counterpart: pgeof has no serving layer).
+ * `slots` worker threads, each with its own CUDA stream, admit requests in
+ * arrival order as soon as a slot is free and the request's device-memory
+ * footprint fits in `budget_bytes` next to the requests in flight (a request
+ * larger than the budget runs alone), so requests overlap on the GPU. Each
+ * request runs pgeof_host_compute_features_selected_f32/_f64 with its own
+ * HOST buffers, which must stay valid until pgeof_server_wait returns for it;
+ * its result equals that call made alone.
+ * create: on the current device. submit: enqueues and returns at once.
+ * wait: blocks until the request is done, returns ITS status (argument and
+ * data errors of the call) and forgets it; latency_ms = submit to done,
+ * queue_ms = submit to admission, slot = the worker that ran it (each may be
+ * NULL). destroy: finishes queued and in-flight requests, joins the workers. */
+typedef struct pgeof_server_s* pgeof_server;
+int pgeof_server_create(int slots, uint64_t budget_bytes, pgeof_server* out);
+int pgeof_server_submit_selected_f32(pgeof_server server, const float* xyz, int64_t n, float search_radius,
+                                     uint32_t max_knn, const int32_t* selected, int64_t n_selected, float* features,
+                                     uint64_t* request_id);
+int pgeof_server_submit_selected_f64(pgeof_server server, const double* xyz, int64_t n, double search_radius,
+                                     uint32_t max_knn, const int32_t* selected, int64_t n_selected, double* features,
+                                     uint64_t* request_id);
+int pgeof_server_wait(pgeof_server server, uint64_t request_id, double* latency_ms, double* queue_ms, int* slot);
+int pgeof_server_stats(pgeof_server server, uint64_t* peak_bytes, int* peak_in_flight, uint64_t* completed);
+int pgeof_server_destroy(pgeof_server server);
+
 /* ------------------------------------------------ resident cloud index */
 /* The reference rebuilds its KD-tree inside every search call
  * (include/nn_search.hpp:35,39,90,97; include/pgeof.hpp:330,333); a resident

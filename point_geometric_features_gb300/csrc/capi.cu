@@ -353,22 +353,59 @@ int eig_order() { return g_eig_order.load(std::memory_order_relaxed); }
 using namespace pgeof;
 
 namespace {
+bool page_locked(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// A block of the page-locked host cache, returned to it on scope exit.
+struct HostBlock {
+    void* p = nullptr;
+    ~HostBlock() {
+        if (p) pgeof_host_free(p);
+    }
+    int alloc(size_t bytes) { return pgeof_host_alloc(bytes, &p); }
+};
+
 template <typename T>
 int host_selected(const T* xyz, int64_t n, T radius, uint32_t max_knn, const int32_t* ids, int64_t n_ids,
                          T* features) {
     PGEOF_TRY(check_cloud(n, "xyz"));
     if (n_ids < 0 || (n_ids > 0 && !ids)) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid selected feature list");
     if (n == 0 || n_ids == 0) return PGEOF_OK;
+    // Pageable caller arrays are staged through page-locked blocks: the copies
+    // then run asynchronously at full speed, and concurrent calls (a request
+    // server's slots) do not queue on the driver's own pageable staging.
+    const uint64_t cnt = (uint64_t)n * n_ids;
+    HostBlock in_stage, out_stage;
+    const T* src = xyz;
+    T* dst = features;
+    if (!page_locked(xyz) && in_stage.alloc(3ull * n * sizeof(T)) == PGEOF_OK) {
+        std::memcpy(in_stage.p, xyz, 3ull * n * sizeof(T));
+        src = static_cast<const T*>(in_stage.p);
+    }
+    if (!page_locked(features) && out_stage.alloc(cnt * sizeof(T)) == PGEOF_OK) dst = static_cast<T*>(out_stage.p);
     const cudaStream_t s = host_stream();
     CallErrors ce(s);
     PGEOF_TRY(ce.begin());
     Scratch d_xyz, d_out;
-    PGEOF_TRY(upload(d_xyz, xyz, 3ull * n, s));
-    const uint64_t cnt = (uint64_t)n * n_ids;
-    PGEOF_TRY(d_out.alloc(cnt * sizeof(T), s));
-    PGEOF_TRY(selected_impl<T>(d_xyz.as<T>(), n, radius, max_knn, ids, n_ids, d_out.as<T>(), s));
-    PGEOF_TRY(download(features, d_out, cnt, s));
-    return finish_host(ce, s);
+    const int st = [&] {
+        PGEOF_TRY(upload(d_xyz, src, 3ull * n, s));
+        PGEOF_TRY(d_out.alloc(cnt * sizeof(T), s));
+        PGEOF_TRY(selected_impl<T>(d_xyz.as<T>(), n, radius, max_knn, ids, n_ids, d_out.as<T>(), s));
+        PGEOF_TRY(download(dst, d_out, cnt, s));
+        return finish_host(ce, s);
+    }();
+    if (st != PGEOF_OK) {
+        cudaStreamSynchronize(s);  // no copy may still touch the staging blocks
+        return st;
+    }
+    if (dst != features) std::memcpy(features, dst, cnt * sizeof(T));
+    return PGEOF_OK;
 }
 
 struct OccEntry {

@@ -418,6 +418,43 @@ PYBIND11_MODULE(pgeof_ext, m) {
     m.def("_batch_plan_destroy", [](uintptr_t plan) {
         check(pgeof_batch_plan_destroy(reinterpret_cast<pgeof_batch_plan>(plan)));
     });
+    m.def("_server_create", [](int slots, uint64_t budget) {
+        pgeof_server sv = nullptr;
+        check(pgeof_server_create(slots, budget, &sv));
+        return reinterpret_cast<uintptr_t>(sv);
+    });
+    m.def("_server_submit", [](uintptr_t sv, uintptr_t xyz, int64_t n, double r, uint32_t max_knn,
+                               const std::vector<int32_t>& ids, uintptr_t out, bool f64) {
+        uint64_t id = 0;
+        if (f64)
+            check(pgeof_server_submit_selected_f64(reinterpret_cast<pgeof_server>(sv), P<const double>(xyz), n, r,
+                                                   max_knn, ids.data(), (int64_t)ids.size(), P<double>(out), &id));
+        else
+            check(pgeof_server_submit_selected_f32(reinterpret_cast<pgeof_server>(sv), P<const float>(xyz), n,
+                                                   (float)r, max_knn, ids.data(), (int64_t)ids.size(), P<float>(out),
+                                                   &id));
+        return id;
+    });
+    m.def("_server_wait", [](uintptr_t sv, uint64_t id) {
+        double lat = 0.0, qms = 0.0;
+        int slot = -1, st;
+        {
+            py::gil_scoped_release nogil;
+            st = pgeof_server_wait(reinterpret_cast<pgeof_server>(sv), id, &lat, &qms, &slot);
+        }
+        check(st);
+        return py::make_tuple(lat, qms, slot);
+    });
+    m.def("_server_stats", [](uintptr_t sv) {
+        uint64_t peak = 0, done = 0;
+        int peak_n = 0;
+        check(pgeof_server_stats(reinterpret_cast<pgeof_server>(sv), &peak, &peak_n, &done));
+        return py::make_tuple(peak, peak_n, done);
+    });
+    m.def("_server_destroy", [](uintptr_t sv) {
+        py::gil_scoped_release nogil;
+        check(pgeof_server_destroy(reinterpret_cast<pgeof_server>(sv)));
+    });
     m.def("_index_create", [](uintptr_t data, int64_t n, uint32_t k_hint, float radius_hint, uintptr_t stream) {
         pgeof_index ix = nullptr;
         int st;

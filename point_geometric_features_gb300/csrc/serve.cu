@@ -1,0 +1,232 @@
+// serve.cu -- native request server (pgeof_server_*) for
+// compute_features_selected (include/pgeof.hpp:325-375); the reference has no
+// serving layer.
+//
+// Continuous batching: `slots` worker threads, each with its own CUDA stream
+// (the host-pointer API keeps one stream per host thread), take requests from
+// one FIFO queue as soon as a slot is free and the request's device-memory
+// footprint fits next to what is in flight, so requests that arrive while
+// others run start at once and their kernels overlap on the GPU. A request
+// runs exactly the synchronous host call (upload, radius grid, fused radius
+// search, PCA, selected features, download); results do not depend on what
+// else is in flight. No Python and no GIL on this path: submit() enqueues and
+// returns, wait() blocks on the request alone.
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace pgeof {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct ServeRequest {
+    uint64_t id = 0;
+    bool f64 = false;
+    const void* xyz = nullptr;
+    int64_t n = 0;
+    double radius = 0.0;
+    uint32_t max_knn = 0;
+    std::vector<int32_t> ids;
+    void* out = nullptr;
+    uint64_t footprint = 0;
+    int slot = -1;
+    Clock::time_point t_submit, t_admit, t_done;
+    int status = PGEOF_OK;
+    std::string msg;
+    bool done = false;
+};
+
+// Device bytes a request holds while in flight (upper bound): input, the
+// cell-sorted copy, the grid build's keys and cell table, the neighbour table,
+// the counts and the output, plus 1 MiB of fixed scratch.
+uint64_t footprint(int64_t n, uint32_t max_knn, int64_t n_ids, bool f64) {
+    const uint64_t real = f64 ? 8 : 4;
+    const uint64_t per_point = 3 * real + (f64 ? 32 : 16) + 16 + 20 + 4ull * std::max<uint32_t>(max_knn, 1) + 4 +
+                               real * (uint64_t)n_ids;
+    return (uint64_t)n * per_point + (1ull << 20);
+}
+
+struct Server {
+    int device = 0;
+    uint64_t budget = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<ServeRequest>> queue;
+    std::unordered_map<uint64_t, std::shared_ptr<ServeRequest>> table;
+    std::vector<int> free_slots;
+    uint64_t next_id = 1, in_use = 0, peak_bytes = 0, completed = 0;
+    int in_flight = 0, peak_in_flight = 0;
+    bool stopping = false;
+    std::vector<std::thread> workers;
+
+    void worker() {
+        cudaSetDevice(device);
+        for (;;) {
+            std::shared_ptr<ServeRequest> r;
+            uint64_t fp = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                // FIFO admission: the oldest request runs as soon as a slot and
+                // its footprint are free (a request larger than the budget runs
+                // alone)
+                cv_work.wait(lk, [&] {
+                    if (queue.empty()) return stopping;
+                    fp = std::min(queue.front()->footprint, budget);
+                    return !free_slots.empty() && in_use + fp <= budget;
+                });
+                if (queue.empty()) return;
+                r = queue.front();
+                queue.pop_front();
+                r->slot = free_slots.back();
+                free_slots.pop_back();
+                in_use += fp;
+                ++in_flight;
+                peak_bytes = std::max(peak_bytes, in_use);
+                peak_in_flight = std::max(peak_in_flight, in_flight);
+                r->t_admit = Clock::now();
+            }
+            int st;
+            if (r->f64)
+                st = pgeof_host_compute_features_selected_f64(static_cast<const double*>(r->xyz), r->n, r->radius,
+                                                              r->max_knn, r->ids.data(), (int64_t)r->ids.size(),
+                                                              static_cast<double*>(r->out));
+            else
+                st = pgeof_host_compute_features_selected_f32(static_cast<const float*>(r->xyz), r->n,
+                                                              (float)r->radius, r->max_knn, r->ids.data(),
+                                                              (int64_t)r->ids.size(), static_cast<float*>(r->out));
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                r->status = st;
+                if (st != PGEOF_OK) r->msg = pgeof_last_error_message();
+                r->t_done = Clock::now();
+                r->done = true;
+                in_use -= fp;
+                --in_flight;
+                free_slots.push_back(r->slot);
+                ++completed;
+            }
+            cv_work.notify_all();
+            cv_done.notify_all();
+        }
+    }
+};
+
+int submit(Server* sv, bool f64, const void* xyz, int64_t n, double radius, uint32_t max_knn, const int32_t* ids,
+           int64_t n_ids, void* out, uint64_t* request_id) {
+    if (!sv || !request_id) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid server or NULL request_id");
+    if (n < 0 || n_ids < 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "negative size");
+    if ((n > 0 && (!xyz || (n_ids > 0 && !out))) || (n_ids > 0 && !ids))
+        return fail(PGEOF_ERR_INVALID_ARGUMENT, "NULL buffer");
+    auto r = std::make_shared<ServeRequest>();
+    r->f64 = f64;
+    r->xyz = xyz;
+    r->n = n;
+    r->radius = radius;
+    r->max_knn = max_knn;
+    r->ids.assign(ids, ids + n_ids);
+    r->out = out;
+    r->footprint = footprint(n, max_knn, n_ids, f64);
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->stopping) return fail(PGEOF_ERR_INVALID_ARGUMENT, "the server is shutting down");
+        r->id = sv->next_id++;
+        sv->table.emplace(r->id, r);
+        sv->queue.push_back(r);
+        *request_id = r->id;
+    }
+    sv->cv_work.notify_all();
+    return PGEOF_OK;
+}
+
+}  // namespace
+}  // namespace pgeof
+
+using namespace pgeof;
+
+extern "C" {
+
+int pgeof_server_create(int slots, uint64_t budget_bytes, pgeof_server* out) {
+    if (!out) return fail(PGEOF_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (slots < 1 || slots > 256) return fail(PGEOF_ERR_INVALID_ARGUMENT, "slots must be in [1, 256]");
+    if (budget_bytes == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "budget_bytes must be > 0");
+    Server* sv = new Server();
+    if (cudaGetDevice(&sv->device) != cudaSuccess) {
+        delete sv;
+        return fail(PGEOF_ERR_CUDA, "cudaGetDevice");
+    }
+    sv->budget = budget_bytes;
+    for (int i = slots - 1; i >= 0; --i) sv->free_slots.push_back(i);
+    for (int i = 0; i < slots; ++i) sv->workers.emplace_back([sv] { sv->worker(); });
+    *out = reinterpret_cast<pgeof_server>(sv);
+    return PGEOF_OK;
+}
+
+int pgeof_server_submit_selected_f32(pgeof_server server, const float* xyz, int64_t n, float search_radius,
+                                     uint32_t max_knn, const int32_t* selected, int64_t n_selected, float* features,
+                                     uint64_t* request_id) {
+    return submit(reinterpret_cast<Server*>(server), false, xyz, n, search_radius, max_knn, selected, n_selected,
+                  features, request_id);
+}
+
+int pgeof_server_submit_selected_f64(pgeof_server server, const double* xyz, int64_t n, double search_radius,
+                                     uint32_t max_knn, const int32_t* selected, int64_t n_selected, double* features,
+                                     uint64_t* request_id) {
+    return submit(reinterpret_cast<Server*>(server), true, xyz, n, search_radius, max_knn, selected, n_selected,
+                  features, request_id);
+}
+
+int pgeof_server_wait(pgeof_server server, uint64_t request_id, double* latency_ms, double* queue_ms, int* slot) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid server");
+    std::shared_ptr<ServeRequest> r;
+    {
+        std::unique_lock<std::mutex> lk(sv->mu);
+        auto it = sv->table.find(request_id);
+        if (it == sv->table.end()) return fail(PGEOF_ERR_INVALID_ARGUMENT, "unknown request id");
+        r = it->second;
+        sv->cv_done.wait(lk, [&] { return r->done; });
+        sv->table.erase(it);
+    }
+    using ms = std::chrono::duration<double, std::milli>;
+    if (latency_ms) *latency_ms = ms(r->t_done - r->t_submit).count();
+    if (queue_ms) *queue_ms = ms(r->t_admit - r->t_submit).count();
+    if (slot) *slot = r->slot;
+    if (r->status != PGEOF_OK) return fail(r->status, r->msg);
+    return PGEOF_OK;
+}
+
+int pgeof_server_stats(pgeof_server server, uint64_t* peak_bytes, int* peak_in_flight, uint64_t* completed) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid server");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (peak_bytes) *peak_bytes = sv->peak_bytes;
+    if (peak_in_flight) *peak_in_flight = sv->peak_in_flight;
+    if (completed) *completed = sv->completed;
+    return PGEOF_OK;
+}
+
+int pgeof_server_destroy(pgeof_server server) {
+    Server* sv = reinterpret_cast<Server*>(server);
+    if (!sv) return PGEOF_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stopping = true;
+    }
+    sv->cv_work.notify_all();
+    for (auto& t : sv->workers) t.join();  // queued requests finish first
+    delete sv;
+    return PGEOF_OK;
+}
+
+}  // extern "C"

@@ -23,7 +23,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-__all__ = ["Request", "Result", "AdmissionControl", "Server", "request_footprint", "radius_for_count"]
+__all__ = ["Request", "Result", "AdmissionControl", "Server", "NativeServer", "request_footprint",
+           "radius_for_count"]
 
 
 @dataclass
@@ -195,6 +196,76 @@ class Server:
             with self.lock:
                 self.results.append(Result(req.rid, feats, req.arrival, admitted, time.perf_counter(),
                                            req.xyz.shape[0], slot))
+
+
+class _NativePeaks:
+    """peak_bytes / peak_in_flight of a NativeServer, read from the library."""
+
+    def __init__(self, server):
+        self._server = server
+
+    @property
+    def peak_bytes(self) -> int:
+        return int(self._server._stats()[0])
+
+    @property
+    def peak_in_flight(self) -> int:
+        return int(self._server._stats()[1])
+
+
+class NativeServer:
+    """The same continuous-batching server as ``Server``, run by the library
+    itself (pgeof_server_*: C++ worker threads, one CUDA stream each, FIFO
+    admission within the device-memory budget): no Python on the request path.
+    submit() enqueues the request with its host arrays; drain() waits for the
+    results, whose latencies the library timestamps."""
+
+    def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, device: int = 0):
+        import torch
+
+        from . import pgeof_ext
+
+        self._ext = pgeof_ext
+        with torch.cuda.device(device):
+            self._h = pgeof_ext._server_create(int(slots), int(budget_bytes))
+        self._inflight: dict = {}  # request id -> (Request, output array), kept alive until waited on
+        self.results: list[Result] = []
+        self.adm = _NativePeaks(self)
+
+    def _stats(self):
+        return self._ext._server_stats(self._h)
+
+    def submit(self, req: Request) -> None:
+        if not req.arrival:
+            req.arrival = time.perf_counter()
+        xyz = np.ascontiguousarray(req.xyz)
+        f64 = xyz.dtype == np.float64
+        if not f64 and xyz.dtype != np.float32:
+            raise TypeError("xyz must be float32 or float64")
+        ids = [int(v) for v in req.features]
+        out = np.zeros((xyz.shape[0], len(ids)), xyz.dtype)
+        rid = self._ext._server_submit(self._h, xyz.ctypes.data, xyz.shape[0], float(req.radius), int(req.max_knn),
+                                       ids, out.ctypes.data, f64)
+        self._inflight[rid] = (req, xyz, out)
+
+    def drain(self, n_expected: int | None = None, timeout: float = 600.0) -> list[Result]:
+        for rid in sorted(self._inflight):
+            req, xyz, out = self._inflight.pop(rid)
+            lat, qms, slot = self._ext._server_wait(self._h, rid)
+            self.results.append(Result(req.rid, out, req.arrival, req.arrival + qms / 1e3,
+                                       req.arrival + lat / 1e3, xyz.shape[0], slot))
+        return list(self.results)
+
+    def close(self) -> None:
+        if getattr(self, "_h", 0):
+            self._ext._server_destroy(self._h)
+            self._h = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def summarize(results: list[Result], wall_s: float) -> dict:

@@ -122,3 +122,18 @@ def test_f64_feature_argument_errors_without_device(pgeof):
         pgeof.compute_features_f64(xyz.astype(np.float32), nn, ptr)
     with pytest.raises(TypeError):
         pgeof.compute_features(xyz, nn, ptr)  # the reference's float32-only entry point stays strict
+
+
+def test_server_handle_argument_checks_without_device(pgeof):
+    """pgeof_server_*: argument errors come back before any thread or device work."""
+    lib = ctypes.CDLL(pgeof.LIBRARY_PATH)
+    h = ctypes.c_void_p(0)
+    assert lib.pgeof_server_create(0, ctypes.c_uint64(1 << 30), ctypes.byref(h)) == 1
+    assert lib.pgeof_server_create(4, ctypes.c_uint64(0), ctypes.byref(h)) == 1
+    assert lib.pgeof_server_create(4, ctypes.c_uint64(1 << 30), None) == 1
+    rid = ctypes.c_uint64(0)
+    assert lib.pgeof_server_submit_selected_f32(None, None, ctypes.c_int64(0), ctypes.c_float(1.0), 4, None,
+                                                ctypes.c_int64(0), None, ctypes.byref(rid)) == 1
+    assert lib.pgeof_server_wait(None, ctypes.c_uint64(1), None, None, None) == 1
+    assert lib.pgeof_server_stats(None, None, None, None) == 1
+    assert lib.pgeof_server_destroy(None) == 0

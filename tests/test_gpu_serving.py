@@ -52,3 +52,70 @@ def test_poisson_stream_summary(cuda, pgeof):
     assert out["requests"] > 60
     assert 0 < out["p50_ms"] <= out["p99_ms"] < 5_000
     assert out["points_per_s"] > 0
+
+
+def test_native_server_results_same_alone_and_in_the_mix(cuda, pgeof):
+    """The library's own server (pgeof_server_*): float32 and float64 requests
+    in one burst overlap on the GPU and each equals the call made alone."""
+    from point_geometric_features_gb300.serving import NativeServer, Request, radius_for_count
+
+    pool = _pool(10, 1_000, 60_000, seed=9)
+    rng = np.random.default_rng(10)
+    feats = [pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z, pgeof.Eigentropy]
+    reqs = []
+    for i in range(40):
+        xyz = pool[int(rng.integers(len(pool)))]
+        if i % 4 == 3:
+            xyz = xyz.astype(np.float64)
+        k = int(rng.choice([16, 32, 64]))
+        reqs.append(Request(i, xyz, k, radius_for_count(xyz, 1.5 * k), feats))
+    alone = {r.rid: pgeof.compute_features_selected(r.xyz, r.radius, r.max_knn, feats) for r in reqs}
+    server = NativeServer(slots=4, budget_bytes=2 << 30)
+    try:
+        for r in reqs:
+            server.submit(r)
+        results = server.drain(len(reqs))
+        assert server.adm.peak_in_flight > 1
+        assert 0 < server.adm.peak_bytes <= 2 << 30
+    finally:
+        server.close()
+    assert len(results) == len(reqs) and len({r.slot for r in results}) > 1
+    for res in results:
+        assert res.features.dtype == alone[res.rid].dtype
+        np.testing.assert_array_equal(res.features, alone[res.rid])
+        assert res.done >= res.admitted >= res.arrival
+
+
+def test_native_server_reports_request_errors(cuda, pgeof):
+    from point_geometric_features_gb300.serving import NativeServer, Request
+
+    pool = _pool(2, 1_000, 2_000, seed=11)
+    server = NativeServer(slots=2, budget_bytes=1 << 30)
+    try:
+        server.submit(Request(0, pool[0], 16, 1.0, [pgeof.Linearity]))
+        bad = pool[1].copy()
+        bad[0, 0] = np.inf  # rejected after the bounding box, before any cell is indexed
+        server.submit(Request(1, bad, 16, 1.0, [pgeof.Linearity]))
+        server.submit(Request(2, pool[1], 16, 1.0, [pgeof.Linearity]))
+        with pytest.raises(ValueError, match="coordinates must be finite"):
+            server.drain(3)
+        res = server.drain(3)  # the other requests still complete
+    finally:
+        server.close()
+    assert sorted(r.rid for r in res) == [0, 2]
+    np.testing.assert_array_equal(res[-1].features, pgeof.compute_features_selected(pool[1], 1.0, 16,
+                                                                                   [pgeof.Linearity]))
+
+
+def test_native_poisson_stream_summary(cuda, pgeof):
+    from point_geometric_features_gb300.serving import NativeServer, run_stream
+
+    pool = _pool(8, 1_000, 50_000, seed=7)
+    server = NativeServer(slots=4, budget_bytes=4 << 30)
+    try:
+        out = run_stream(server, pool, rate=60.0, duration=2.0, seed=8)
+    finally:
+        server.close()
+    assert out["requests"] > 60
+    assert 0 < out["p50_ms"] <= out["p99_ms"] < 5_000
+    assert out["peak_in_flight_requests"] >= 1
