@@ -61,11 +61,11 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--skip-e2e", action="store_true", help="device timing only (profiling runs)")
-    p.add_argument("--workload", choices=["scene", "features", "batch", "serve", "optimal", "index"], default="scene",
+    p.add_argument("--workload", choices=["scene", "features", "batch", "serve", "optimal", "index", "refbench"], default="scene",
                    help="scene: the headline 1M-point kNN+multiscale step; features: the 1M-point k=50 "
                         "compute_features pass alone; batch: 256 clouds, plain vs batched; serve: Poisson request "
                         "stream with p50/p99 latency; optimal: 4M-point radius -> optimal-k; index: searches on one "
-                        "resident grid vs per-call grids")
+                        "resident grid vs per-call grids; refbench: the reference's own benchmark shapes")
     p.add_argument("--points", type=int, default=None,
                    help="scene / features: cloud size (default 1,000,000; e.g. 4M and 16M for the asymptote)")
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
@@ -688,6 +688,58 @@ def run_index(args):
     }
 
 
+def run_refbench(args):
+    """The reference's own benchmark shapes, for continuity
+    (tests/bench_knn.py, tests/bench_jakteristics.py of the reference),
+    through the numpy drop-in API as those benchmarks call it: 1M points
+    uniform in [0, 200)^3 (seeded here) -> knn_search(k=50) and
+    radius_search(r=0.2, max_knn=30); 10k float64 points in [0, 200)^3 ->
+    compute_features_selected(r=5, max_knn=50, [Verticality]). Median of
+    `steps` calls after `warmup`; the reference benches' own comparator
+    (scipy's cKDTree, all host threads) is timed beside the two searches."""
+    import time as _t
+
+    import point_geometric_features_gb300 as pgeof
+    from scipy.spatial import cKDTree
+
+    rng = np.random.default_rng(0)
+    xyz = rng.uniform(0.0, 200.0, size=(1_000_000, 3)).astype(np.float32)
+    small = rng.uniform(0.0, 200.0, size=(10_000, 3))
+
+    def med(fn, steps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        ts = []
+        for _ in range(steps):
+            t0 = _t.perf_counter()
+            fn()
+            ts.append((_t.perf_counter() - t0) * 1e3)
+        return float(np.median(ts))
+
+    out = {
+        "knn_search_1M_k50_ms": med(lambda: pgeof.knn_search(xyz, xyz, 50), args.steps),
+        "radius_search_1M_r0.2_max30_ms": med(lambda: pgeof.radius_search(xyz, xyz, 0.2, 30), args.steps),
+        "selected_10k_f64_r5_max50_ms": med(
+            lambda: pgeof.compute_features_selected(small, 5.0, 50, [pgeof.Verticality]), args.steps),
+    }
+    if not args.no_cpu_baseline:
+        def scipy_knn():
+            cKDTree(xyz).query(xyz, k=50, workers=-1)
+
+        def scipy_radius():
+            cKDTree(xyz).query(xyz, k=30, distance_upper_bound=0.2, workers=-1)
+
+        out["scipy_knn_1M_k50_ms"] = med(scipy_knn, 2)
+        out["scipy_radius_1M_r0.2_max30_ms"] = med(scipy_radius, 2)
+    return {
+        "metric": "ms per call, the reference's benchmark shapes (numpy API, host copies inside)",
+        "workload": "refbench", "unit": "ms", "higher_is_better": False, "steps": args.steps, "dtype": "f32/f64",
+        "config": {"workload": "tests/bench_knn.py and tests/bench_jakteristics.py shapes, seeded",
+                   "host_threads": os.cpu_count()},
+        **{k: round(v, 3) for k, v in out.items()},
+    }
+
+
 def main():
     global N_POINTS, WORKLOAD
     args = parse()
@@ -706,6 +758,10 @@ def main():
     if args.workload == "serve" and args.impl == "ours":
         if rank == 0:
             print(json.dumps(run_serve(args)), flush=True)
+        return
+    if args.workload == "refbench" and args.impl == "ours":
+        if rank == 0:
+            print(json.dumps(run_refbench(args)), flush=True)
         return
     if args.workload == "index" and args.impl == "ours":
         if rank == 0:
