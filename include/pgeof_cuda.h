@@ -256,7 +256,9 @@ int pgeof_batch_plan_destroy(pgeof_batch_plan plan);
  * wait: blocks until the request is done, returns ITS status (argument and
  * data errors of the call) and forgets it; latency_ms = submit to done,
  * queue_ms = submit to admission, slot = the worker that ran it (each may be
- * NULL). destroy: finishes queued and in-flight requests, joins the workers. */
+ * NULL). destroy: finishes queued and in-flight requests, joins the workers;
+ * no other call on the same server may run during or after it. submit, wait
+ * and stats are thread-safe. */
 typedef struct pgeof_server_s* pgeof_server;
 int pgeof_server_create(int slots, uint64_t budget_bytes, pgeof_server* out);
 int pgeof_server_submit_selected_f32(pgeof_server server, const float* xyz, int64_t n, float search_radius,
@@ -281,7 +283,9 @@ int pgeof_server_destroy(pgeof_server server);
  * keeps its own cell-ordered copy); k_hint = the neighbour count searches will
  * mostly ask for (0: 16), radius_hint = their radius (0: none). Synchronises
  * `stream`; afterwards any stream of the same device may search the index,
- * concurrently. destroy waits for the searches enqueued so far.
+ * concurrently, and calls from several host threads are safe. destroy waits
+ * for the searches enqueued so far; no call on the index may run during or
+ * after it.
  * query == NULL searches the indexed points themselves (n_query ignored,
  * n_data rows in the cloud's original order): the self-search of
  * knn_search(xyz, xyz, k).
