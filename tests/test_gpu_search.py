@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 from scipy.spatial import KDTree
 
+from conftest import feature_close
 from oracle import oracle
 from point_geometric_features_gb300.synthetic import outdoor_scene, uniform_cube
 
@@ -236,3 +237,22 @@ def test_host_knn_pipeline_large_matches_device_path(cuda, pgeof):
     i_h, d_h = pgeof.knn_search(xyz, q, 40)
     np.testing.assert_array_equal(i_h, i_d.cpu().numpy().astype(np.uint32))
     np.testing.assert_array_equal(d_h, d_d.cpu().numpy())
+
+
+def test_all_points_identical(cuda, pgeof):
+    """A cloud collapsed to one position: every distance is 0, so every row is
+    the lowest indices in order (include/nn_search.hpp:31-132 with the
+    (distance, index) tie order) and the grid has a single cell."""
+    xyz = np.full((3000, 3), 0.25, np.float32)
+    for k in (1, 50, 200):
+        idx, d2 = pgeof.knn_search(xyz, xyz, k)
+        assert np.all(d2 == 0)
+        np.testing.assert_array_equal(idx, np.broadcast_to(np.arange(k, dtype=np.uint32), idx.shape))
+    idx, d2 = pgeof.radius_search(xyz, xyz, 0.1, 64)
+    np.testing.assert_array_equal(idx, np.broadcast_to(np.arange(64, dtype=np.int32), idx.shape))
+    ri, rd = oracle.radius_search(xyz, xyz[:50], 0.1, 64)
+    np.testing.assert_array_equal(idx[:50], ri)
+    np.testing.assert_array_equal(d2[:50], rd)
+    nn = idx[:, :20].reshape(-1).astype(np.uint32)
+    ptr = (np.arange(xyz.shape[0] + 1) * 20).astype(np.uint32)
+    assert feature_close(pgeof.compute_features(xyz, nn, ptr), oracle.compute_features(xyz, nn, ptr)).all()
