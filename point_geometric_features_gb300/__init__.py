@@ -139,6 +139,19 @@ def _uint32_empty(torch, shape, device):
     return torch.empty(shape, dtype=torch.int32, device=device)
 
 
+def _to_host(t, as_uint32=False):
+    """A CUDA tensor as a numpy array in page-locked memory from torch's cached
+    host allocator: the download runs at DMA speed instead of page-faulting a
+    fresh pageable array (the numpy array keeps the block alive)."""
+    torch = _sys.modules["torch"]
+    if as_uint32 or t.dtype not in (torch.float32, torch.float64, torch.int32, torch.int64):
+        t = t.view(torch.int32)
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    a = h.numpy()
+    return a.view("uint32") if as_uint32 else a
+
+
 def _finish(check, stream):
     if check:
         check_device_errors(stream)
@@ -306,7 +319,7 @@ def radius_search_csr(data, query, search_radius, max_knn):
         nnz = int(nn_ptr[m:].view(torch.int32).item())
     nn = nn[:nnz]
     if numpy_in:
-        return nn.view(torch.int32).cpu().numpy().view("uint32"), nn_ptr.view(torch.int32).cpu().numpy().view("uint32")
+        return _to_host(nn, True), _to_host(nn_ptr, True)
     return nn, nn_ptr
 
 
@@ -339,7 +352,7 @@ def knn_features(xyz, k, k_scales=None):
         s = int(torch.cuda.current_stream().cuda_stream)
         out = torch.zeros(shape, dtype=torch.float32, device=t.device)
         _ext._dev_knn_features(t.data_ptr(), n, int(k), scales, out.data_ptr(), s)
-    return out.cpu().numpy() if numpy_in else out
+    return _to_host(out) if numpy_in else out
 
 
 def compute_features_selected(xyz, search_radius, max_knn, selected_features):
@@ -489,9 +502,7 @@ class GridIndex:
         """Results as given (CUDA tensors) or as numpy arrays for numpy inputs."""
         if not self._numpy:
             return ts if len(ts) > 1 else ts[0]
-        torch = _sys.modules["torch"]
-        res = [ts[0].view(torch.int32).cpu().numpy().view("uint32") if uint32_first else ts[0].cpu().numpy()]
-        res += [t.cpu().numpy() for t in ts[1:]]
+        res = [_to_host(ts[0], uint32_first)] + [_to_host(t) for t in ts[1:]]
         return tuple(res) if len(res) > 1 else res[0]
 
     def knn_search(self, query, knn):
