@@ -71,6 +71,8 @@ def parse():
     p.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     p.add_argument("--server", choices=["native", "python"], default="native",
                    help="serve: the library's C++ request server or the Python one")
+    p.add_argument("--resident", action="store_true",
+                   help="serve: keep the request pool's clouds resident in the server (repeated queries)")
     p.add_argument("--rate", type=float, default=200.0, help="serve: requests per second")
     return p.parse_args()
 
@@ -512,11 +514,14 @@ def run_serve(args):
     rng = np.random.default_rng(4)
     sizes = log_uniform_sizes(96, 1_000, 500_000, seed=4)
     pool = [scaled_scene(int(n), seed=4000 + i, side=float(rng.uniform(5.0, 50.0))) for i, n in enumerate(sizes)]
-    server = (NativeServer if args.server == "native" else Server)(slots=8, budget_bytes=40 << 30)
+    server = (NativeServer if args.server == "native" or args.resident else Server)(slots=8, budget_bytes=40 << 30)
+    clouds = None
+    if args.resident:  # the pool's clouds kept on the device; requests run on them
+        clouds = [server.add_cloud(c, k_hint=32) for c in pool]
     try:
-        run_stream(server, pool, rate=args.rate, duration=min(3.0, args.duration), seed=40)  # warm-up
+        run_stream(server, pool, rate=args.rate, duration=min(3.0, args.duration), seed=40, clouds=clouds)  # warm-up
         server.results.clear()
-        out = run_stream(server, pool, rate=args.rate, duration=args.duration, seed=4)
+        out = run_stream(server, pool, rate=args.rate, duration=args.duration, seed=4, clouds=clouds)
     finally:
         server.close()
     return {
@@ -525,8 +530,10 @@ def run_serve(args):
         "config": {"rate_per_s": args.rate, "duration_s": args.duration, "sizes": "log-uniform [1000, 500000]",
                    "k": [16, 32, 64], "features": ["Verticality", "Curvature", "Planarity", "Normal_z"],
                    "budget_bytes": 40 << 30, "slots": 8,
-                   "server": "library (pgeof_server_*, C++ workers)" if args.server == "native"
-                   else "Python (serving.Server, torch streams)"},
+                   "server": "library (pgeof_server_*, C++ workers)" if args.server == "native" or args.resident
+                   else "Python (serving.Server, torch streams)",
+                   "clouds": "resident on the device (add_cloud), requests name them" if args.resident
+                   else "each request uploads its cloud and builds its grid"},
         "p50_ms": round(out["p50_ms"], 3),
         "p99_ms": round(out["p99_ms"], 3),
         "mean_ms": round(out["mean_ms"], 3),

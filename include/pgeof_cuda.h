@@ -267,6 +267,19 @@ int pgeof_server_submit_selected_f32(pgeof_server server, const float* xyz, int6
 int pgeof_server_submit_selected_f64(pgeof_server server, const double* xyz, int64_t n, double search_radius,
                                      uint32_t max_knn, const int32_t* selected, int64_t n_selected, double* features,
                                      uint64_t* request_id);
+/* Resident clouds: add_cloud uploads a float32 cloud and builds its grid once
+ * (synchronous; radius_hint / k_hint choose the cell size as the per-call
+ * radius path does, results never depend on them) and reserves its device
+ * bytes from the budget; requests submitted with its id skip the upload and
+ * the grid build and return exactly what the call on the same xyz returns.
+ * remove_cloud refuses new requests on it, waits for the queued ones and
+ * releases its bytes. The caller's xyz is not referenced after add_cloud. */
+int pgeof_server_add_cloud_f32(pgeof_server server, const float* xyz, int64_t n, float radius_hint,
+                               uint32_t k_hint, uint64_t* cloud_id);
+int pgeof_server_remove_cloud(pgeof_server server, uint64_t cloud_id);
+int pgeof_server_submit_selected_resident_f32(pgeof_server server, uint64_t cloud_id, float search_radius,
+                                              uint32_t max_knn, const int32_t* selected, int64_t n_selected,
+                                              float* features, uint64_t* request_id);
 int pgeof_server_wait(pgeof_server server, uint64_t request_id, double* latency_ms, double* queue_ms, int* slot);
 int pgeof_server_stats(pgeof_server server, uint64_t* peak_bytes, int* peak_in_flight, uint64_t* completed);
 int pgeof_server_destroy(pgeof_server server);

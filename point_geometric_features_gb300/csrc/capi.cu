@@ -249,14 +249,12 @@ int features_impl(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t
                            (int)n_scales, out, nullptr, s);
 }
 
+// include/pgeof.hpp:325-375 on an existing grid of xyz: radius table (the
+// nearest max_knn inside the radius, uncapped counts), then PCA + features.
 template <typename T>
-int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const int32_t* ids, int64_t n_ids, T* out,
-                  cudaStream_t s) {
-    if (n == 0 || n_ids == 0) return PGEOF_OK;
-    GridIndex<T> grid;
-    const float r = (float)std::fabs((double)radius);
+int selected_on_grid(const GridIndex<T>& grid, const T* xyz, uint64_t n, T radius, uint32_t max_knn,
+                     const int32_t* ids, int64_t n_ids, T* out, cudaStream_t s) {
     const uint32_t k_search = std::max<uint32_t>(max_knn, 1u);
-    PGEOF_TRY(build_grid<T>(xyz, n, k_search, r / 4.0f, r, grid, s));
     Scratch nbr, found;
     PGEOF_TRY(nbr.alloc(n * (uint64_t)k_search * sizeof(int32_t), s));
     PGEOF_TRY(found.alloc(n * sizeof(uint32_t), s));
@@ -268,6 +266,16 @@ int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const in
     PGEOF_TRY(launch_search<T>(grid, grid.pts, grid.cell_start, n, MODE_RADIUS, k_search, radius, so, s));
     return launch_selected_pca<T>(xyz, n, nbr.as<int32_t>(), found.as<uint32_t>(), max_knn, ids, (int)n_ids, out,
                                   s);
+}
+
+template <typename T>
+int selected_impl(const T* xyz, uint64_t n, T radius, uint32_t max_knn, const int32_t* ids, int64_t n_ids, T* out,
+                  cudaStream_t s) {
+    if (n == 0 || n_ids == 0) return PGEOF_OK;
+    GridIndex<T> grid;
+    const float r = (float)std::fabs((double)radius);
+    PGEOF_TRY(build_grid<T>(xyz, n, std::max<uint32_t>(max_knn, 1u), r / 4.0f, r, grid, s));
+    return selected_on_grid<T>(grid, xyz, n, radius, max_knn, ids, n_ids, out, s);
 }
 
 }  // namespace
@@ -463,6 +471,48 @@ int pgeof::kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* 
 }
 
 // =========================================================================
+// ------------------------------------------------ resident clouds (serve.cu)
+int pgeof::resident_cloud_build(const float* xyz, uint64_t n, float radius_hint, uint32_t k_hint,
+                                ResidentCloud& out) {
+    if (n == 0) return fail(PGEOF_ERR_INVALID_ARGUMENT, "a resident cloud needs at least one point");
+    PGEOF_TRY(check_cloud((int64_t)n, "xyz"));
+    const cudaStream_t s = host_stream();
+    out.n = n;
+    PGEOF_TRY(upload(out.xyz, xyz, 3ull * n, s));
+    const float r = std::fabs(radius_hint);
+    PGEOF_TRY(build_grid<float>(out.xyz.as<float>(), n, std::max<uint32_t>(k_hint, 1u), r / 4.0f, r, out.grid, s));
+    PGEOF_CUDA_TRY(cudaStreamSynchronize(s));  // complete before any other stream reads it
+    return PGEOF_OK;
+}
+
+int pgeof::host_selected_resident(const ResidentCloud& c, float radius, uint32_t max_knn, const int32_t* ids,
+                                  int64_t n_ids, float* features) {
+    if (n_ids < 0 || (n_ids > 0 && !ids)) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid selected feature list");
+    if (c.n == 0 || n_ids == 0) return PGEOF_OK;
+    const uint64_t cnt = c.n * (uint64_t)n_ids;
+    HostBlock out_stage;
+    float* dst = features;
+    if (!page_locked(features) && out_stage.alloc(cnt * sizeof(float)) == PGEOF_OK)
+        dst = static_cast<float*>(out_stage.p);
+    const cudaStream_t s = host_stream();
+    CallErrors ce(s);
+    PGEOF_TRY(ce.begin());
+    Scratch d_out;
+    const int st = [&] {
+        PGEOF_TRY(d_out.alloc(cnt * sizeof(float), s));
+        PGEOF_TRY(selected_on_grid<float>(c.grid, c.xyz.as<float>(), c.n, radius, max_knn, ids, n_ids,
+                                          d_out.as<float>(), s));
+        PGEOF_TRY(download(dst, d_out, cnt, s));
+        return finish_host(ce, s);
+    }();
+    if (st != PGEOF_OK) {
+        cudaStreamSynchronize(s);
+        return st;
+    }
+    if (dst != features) std::memcpy(features, dst, cnt * sizeof(float));
+    return PGEOF_OK;
+}
+
 extern "C" {
 
 int pgeof_abi_version(void) { return PGEOF_ABI_VERSION; }

@@ -175,6 +175,20 @@ int exclusive_scan_into(const uint32_t* in, uint32_t G, uint32_t* out, uint32_t*
 int launch_csr_from_table(const int32_t* table, const uint32_t* found, uint64_t m, uint32_t max_knn,
                           uint32_t* counts, uint32_t* partials, uint32_t* nn_ptr, uint32_t* nn, cudaStream_t s);
 
+// A float32 cloud kept on the device with its grid, for repeated
+// compute_features_selected requests (request server).
+struct ResidentCloud {
+    uint64_t n = 0;
+    Scratch xyz;  // (n, 3) float32, original order
+    GridIndex<float> grid;
+};
+// Upload + grid build on the calling thread's host stream; synchronous.
+int resident_cloud_build(const float* xyz, uint64_t n, float radius_hint, uint32_t k_hint, ResidentCloud& out);
+// compute_features_selected on a resident cloud; `features` is host memory,
+// synchronous on the calling thread's host stream.
+int host_selected_resident(const ResidentCloud& c, float radius, uint32_t max_knn, const int32_t* ids,
+                           int64_t n_ids, float* features);
+
 // PCA + selected features from a radius-search neighbour table (selected path).
 template <typename T>
 int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint32_t* found, uint32_t max_knn,

@@ -435,6 +435,28 @@ PYBIND11_MODULE(pgeof_ext, m) {
                                                    &id));
         return id;
     });
+    m.def("_server_add_cloud", [](uintptr_t sv, uintptr_t xyz, int64_t n, float radius_hint, uint32_t k_hint) {
+        uint64_t cid = 0;
+        int st;
+        {
+            py::gil_scoped_release nogil;
+            st = pgeof_server_add_cloud_f32(reinterpret_cast<pgeof_server>(sv), P<const float>(xyz), n, radius_hint,
+                                            k_hint, &cid);
+        }
+        check(st);
+        return cid;
+    });
+    m.def("_server_remove_cloud", [](uintptr_t sv, uint64_t cid) {
+        py::gil_scoped_release nogil;
+        check(pgeof_server_remove_cloud(reinterpret_cast<pgeof_server>(sv), cid));
+    });
+    m.def("_server_submit_resident", [](uintptr_t sv, uint64_t cid, double r, uint32_t max_knn,
+                                        const std::vector<int32_t>& ids, uintptr_t out) {
+        uint64_t id = 0;
+        check(pgeof_server_submit_selected_resident_f32(reinterpret_cast<pgeof_server>(sv), cid, (float)r, max_knn,
+                                                        ids.data(), (int64_t)ids.size(), P<float>(out), &id));
+        return id;
+    });
     m.def("_server_wait", [](uintptr_t sv, uint64_t id) {
         double lat = 0.0, qms = 0.0;
         int slot = -1, st;

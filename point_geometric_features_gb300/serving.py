@@ -35,6 +35,7 @@ class Request:
     radius: float
     features: list
     arrival: float = 0.0  # time.perf_counter() at arrival
+    cloud: int = 0  # NativeServer: id of a resident cloud (add_cloud) to run on instead of xyz
 
 
 @dataclass
@@ -228,16 +229,43 @@ class NativeServer:
         self._ext = pgeof_ext
         with torch.cuda.device(device):
             self._h = pgeof_ext._server_create(int(slots), int(budget_bytes))
-        self._inflight: dict = {}  # request id -> (Request, output array), kept alive until waited on
+        self._inflight: dict = {}  # request id -> (Request, xyz, output array), kept alive until waited on
+        self._clouds: dict = {}  # resident cloud id -> point count
         self.results: list[Result] = []
         self.adm = _NativePeaks(self)
 
     def _stats(self):
         return self._ext._server_stats(self._h)
 
+    def add_cloud(self, xyz: np.ndarray, radius_hint: float = 0.0, k_hint: int = 16) -> int:
+        """Keep a float32 cloud and its grid on the device for repeated
+        requests (Request(cloud=id)); returns its id. Its bytes are reserved
+        from the budget until remove_cloud()."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+        if xyz.ndim != 2 or xyz.shape[1] != 3:
+            raise TypeError("xyz must be a (n, 3) array")
+        cid = self._ext._server_add_cloud(self._h, xyz.ctypes.data, xyz.shape[0], float(radius_hint), int(k_hint))
+        self._clouds[cid] = xyz.shape[0]
+        return cid
+
+    def remove_cloud(self, cid: int) -> None:
+        """Refuse new requests on the cloud, wait for its queued ones, free it."""
+        self._ext._server_remove_cloud(self._h, int(cid))
+        self._clouds.pop(int(cid), None)
+
     def submit(self, req: Request) -> None:
         if not req.arrival:
             req.arrival = time.perf_counter()
+        if req.cloud:
+            ids = [int(v) for v in req.features]
+            n = self._clouds.get(int(req.cloud))
+            if n is None:
+                raise ValueError("unknown resident cloud id")
+            out = np.zeros((n, len(ids)), np.float32)
+            rid = self._ext._server_submit_resident(self._h, int(req.cloud), float(req.radius), int(req.max_knn),
+                                                    ids, out.ctypes.data)
+            self._inflight[rid] = (req, np.empty((n, 0), np.float32), out)
+            return
         xyz = np.ascontiguousarray(req.xyz)
         f64 = xyz.dtype == np.float64
         if not f64 and xyz.dtype != np.float32:
@@ -295,9 +323,11 @@ def poisson_arrivals(rate: float, duration: float, seed: int) -> np.ndarray:
 
 
 def run_stream(server: Server, pool: list, rate: float, duration: float, seed: int, ks=(16, 32, 64),
-               features=None) -> dict:
+               features=None, clouds=None) -> dict:
     """Replay a Poisson stream of requests drawn from `pool` (list of float32
-    clouds) against `server`; returns the latency / throughput summary."""
+    clouds) against `server`; returns the latency / throughput summary.
+    `clouds` (NativeServer): resident cloud ids parallel to `pool`, so that the
+    requests run on the resident copies."""
     import point_geometric_features_gb300 as pgeof
 
     features = features or [pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z]
@@ -305,9 +335,11 @@ def run_stream(server: Server, pool: list, rate: float, duration: float, seed: i
     times = poisson_arrivals(rate, duration, seed)
     reqs = []
     for i, _t in enumerate(times):
-        xyz = pool[int(rng.integers(len(pool)))]
+        j = int(rng.integers(len(pool)))
+        xyz = pool[j]
         k = int(rng.choice(ks))
-        reqs.append(Request(i, xyz, k, radius_for_count(xyz, 1.5 * k), features))
+        reqs.append(Request(i, xyz, k, radius_for_count(xyz, 1.5 * k), features,
+                            cloud=int(clouds[j]) if clouds is not None else 0))
     t0 = time.perf_counter()
     for req, t in zip(reqs, times):
         now = time.perf_counter() - t0

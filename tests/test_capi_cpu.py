@@ -136,4 +136,10 @@ def test_server_handle_argument_checks_without_device(pgeof):
                                                 ctypes.c_int64(0), None, ctypes.byref(rid)) == 1
     assert lib.pgeof_server_wait(None, ctypes.c_uint64(1), None, None, None) == 1
     assert lib.pgeof_server_stats(None, None, None, None) == 1
+    cid = ctypes.c_uint64(0)
+    assert lib.pgeof_server_add_cloud_f32(None, None, ctypes.c_int64(10), ctypes.c_float(1.0), 16,
+                                          ctypes.byref(cid)) == 1
+    assert lib.pgeof_server_remove_cloud(None, ctypes.c_uint64(1)) == 1
+    assert lib.pgeof_server_submit_selected_resident_f32(None, ctypes.c_uint64(1), ctypes.c_float(1.0), 16, None,
+                                                         ctypes.c_int64(0), None, ctypes.byref(rid)) == 1
     assert lib.pgeof_server_destroy(None) == 0

@@ -119,3 +119,39 @@ def test_native_poisson_stream_summary(cuda, pgeof):
     assert out["requests"] > 60
     assert 0 < out["p50_ms"] <= out["p99_ms"] < 5_000
     assert out["peak_in_flight_requests"] >= 1
+
+
+def test_native_server_resident_clouds(cuda, pgeof):
+    """Clouds kept on the device with their grid (add_cloud): repeated requests
+    with other radii, k and feature lists, mixed with plain requests, each
+    equal to compute_features_selected on the same xyz alone."""
+    from point_geometric_features_gb300.serving import NativeServer, Request, radius_for_count
+
+    pool = _pool(6, 2_000, 80_000, seed=12)
+    rng = np.random.default_rng(13)
+    lists = [[pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z],
+             [pgeof.Linearity, pgeof.Eigentropy], [pgeof.Normal_x, pgeof.Normal_y, pgeof.Normal_z, pgeof.Volume]]
+    server = NativeServer(slots=4, budget_bytes=2 << 30)
+    try:
+        cids = [server.add_cloud(pool[i], radius_hint=radius_for_count(pool[i], 48), k_hint=32) for i in range(3)]
+        reqs, expect = [], {}
+        for i in range(36):
+            j = int(rng.integers(len(pool)))
+            k = int(rng.choice([16, 32, 64]))
+            feats = lists[int(rng.integers(len(lists)))]
+            r = radius_for_count(pool[j], float(rng.uniform(0.5, 3.0)) * k)
+            req = Request(i, pool[j], k, r, feats, cloud=cids[j] if j < 3 and i % 3 else 0)
+            reqs.append(req)
+            expect[i] = pgeof.compute_features_selected(pool[j], r, k, feats)
+        for req in reqs:
+            server.submit(req)
+        results = server.drain(len(reqs))
+        assert server.adm.peak_in_flight > 1
+        server.remove_cloud(cids[0])
+        with pytest.raises(ValueError, match="unknown resident cloud"):
+            server.submit(Request(99, None, 16, 1.0, lists[0], cloud=cids[0]))
+    finally:
+        server.close()
+    assert sum(1 for r in reqs if r.cloud) >= 10
+    for res in results:
+        np.testing.assert_array_equal(res.features, expect[res.rid])
