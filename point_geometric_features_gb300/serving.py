@@ -221,14 +221,18 @@ class NativeServer:
     submit() enqueues the request with its host arrays; drain() waits for the
     results, whose latencies the library timestamps."""
 
-    def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, device: int = 0):
-        import torch
+    def __init__(self, slots: int = 8, budget_bytes: int = 40 << 30, device: int = 0, _ext=None):
+        if _ext is not None:  # a stand-in for the library's bindings (host-logic tests)
+            self._ext = _ext
+            self._h = _ext._server_create(int(slots), int(budget_bytes))
+        else:
+            import torch
 
-        from . import pgeof_ext
+            from . import pgeof_ext
 
-        self._ext = pgeof_ext
-        with torch.cuda.device(device):
-            self._h = pgeof_ext._server_create(int(slots), int(budget_bytes))
+            self._ext = pgeof_ext
+            with torch.cuda.device(device):
+                self._h = pgeof_ext._server_create(int(slots), int(budget_bytes))
         self._inflight: dict = {}  # request id -> (Request, xyz, output array), kept alive until waited on
         self._clouds: dict = {}  # resident cloud id -> point count
         self.results: list[Result] = []
