@@ -78,6 +78,9 @@ const char* pgeof_status_string(int status);
 const char* pgeof_last_error_message(void);
 /* Number of kernels this library has launched in this process. */
 uint64_t pgeof_kernel_launch_count(void);
+/* Number of device memory allocations (memory-pool and cudaMalloc) this
+ * library has made in this process. */
+uint64_t pgeof_device_alloc_count(void);
 /* Eigenpair order fed to the feature formulas: 0 = ascending (Eigen's order,
  * what pca.hpp:79-97 does, the default), 1 = descending (val[0] = largest, so
  * v2 is the surface normal). Process-wide. */
@@ -207,14 +210,17 @@ int pgeof_compute_features_selected_f64(const double* xyz, int64_t n, double sea
  * Same arguments, checks and output as pgeof_compute_features_f32, plus
  * `error_bits`: an optional caller-owned device word (zero it first) into
  * which the kernels OR the data-error bits of pgeof_take_device_errors; with
- * NULL they go to a library word that each call clears and no one reads.
+ * NULL they accumulate in a fixed library word for the device, which
+ * pgeof_take_device_errors reads and clears (that call is not itself
+ * allocation-free on its first use on a device).
  * This call makes no cudaMalloc, cudaFree or pool allocation: its scratch (a
  * float4 copy of xyz) is a fixed 16 MiB device array that every GPU loading
  * the library holds until exit, so xyz is limited to 1,048,576 points (more
  * returns PGEOF_ERR_INVALID_ARGUMENT). All calls share that array: calls that
  * overlap on the GPU race and must be serialised by the caller. The first call
  * on each device looks the array's address up (cudaGetSymbolAddress) with that
- * device current; make it before any stream capture. */
+ * device current; make it before any stream capture (a failed lookup is
+ * retried by the next call). */
 int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
                                        const uint32_t* nn_ptr, int64_t n_points, uint64_t k_min, float* features,
                                        uint32_t* error_bits, pgeof_stream_t stream);

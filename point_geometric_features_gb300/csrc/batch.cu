@@ -281,6 +281,7 @@ int workspace_init(BatchWorkspace& w, const int64_t* offsets, int64_t n_clouds, 
         PGEOF_TRY(scratch_alloc(&w.base, bytes, s));
     } else {
         PGEOF_CUDA_TRY(cudaMalloc(&w.base, bytes));
+        count_device_alloc();
     }
     layout(w, (char*)w.base);
     std::vector<uint64_t> off(n_clouds + 1);

@@ -16,6 +16,7 @@
 namespace pgeof {
 
 std::atomic<uint64_t> g_launch_count{0};
+std::atomic<uint64_t> g_device_alloc_count{0};
 
 namespace {
 
@@ -62,7 +63,10 @@ void init_device(DevState& st, int dev) {
         uint64_t keep = ~0ull;
         e = cudaMemPoolSetAttribute(st.pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
-    if (e == cudaSuccess) e = cudaMalloc(&st.err_word, 256);
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&st.err_word, 256);
+        count_device_alloc();
+    }
     if (e == cudaSuccess) e = cudaMemset(st.err_word, 0, 256);
     if (e != cudaSuccess) {
         st.status = PGEOF_ERR_CUDA;
@@ -351,6 +355,7 @@ int scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
     DevState* st;
     PGEOF_TRY(device_state(&st));
     PGEOF_CUDA_TRY(cudaMallocFromPoolAsync(p, bytes, st->pool, s));
+    count_device_alloc();
     return PGEOF_OK;
 }
 void scratch_free(void* p, cudaStream_t s) { cudaFreeAsync(p, s); }
@@ -533,6 +538,7 @@ const char* pgeof_status_string(int status) {
 const char* pgeof_last_error_message(void) { return t_last_error.c_str(); }
 
 uint64_t pgeof_kernel_launch_count(void) { return g_launch_count.load(); }
+uint64_t pgeof_device_alloc_count(void) { return g_device_alloc_count.load(); }
 
 int pgeof_set_eig_order(int order) {
     if (order != 0 && order != 1) return fail(PGEOF_ERR_INVALID_ARGUMENT, "eig order must be 0 or 1");
@@ -601,10 +607,11 @@ int pgeof_take_device_errors(pgeof_stream_t stream, uint32_t* bits) {
     DevState* st;
     PGEOF_TRY(device_state(&st));
     PGEOF_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-    uint32_t v = 0;
+    uint32_t v = 0, v_noalloc = 0;
     PGEOF_CUDA_TRY(cudaMemcpy(&v, st->err_word, sizeof(v), cudaMemcpyDeviceToHost));
     PGEOF_CUDA_TRY(cudaMemset(st->err_word, 0, sizeof(v)));
-    if (bits) *bits = v;
+    PGEOF_TRY(noalloc_take_errors(&v_noalloc));
+    if (bits) *bits = v | v_noalloc;
     return PGEOF_OK;
 }
 

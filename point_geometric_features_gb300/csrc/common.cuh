@@ -43,10 +43,14 @@ enum : uint32_t {
     ERR_INTERNAL = 4u,
 };
 uint32_t* device_error_word();  // per-device word, zeroed at first use
+int noalloc_take_errors(uint32_t* bits);  // reads and clears the no-allocation entry point's word
 
 // ----------------------------------------------------------------- launches
 extern std::atomic<uint64_t> g_launch_count;
 inline void count_launch(uint64_t n = 1) { g_launch_count.fetch_add(n, std::memory_order_relaxed); }
+// device memory allocations made by the library (pool and cudaMalloc)
+extern std::atomic<uint64_t> g_device_alloc_count;
+inline void count_device_alloc() { g_device_alloc_count.fetch_add(1, std::memory_order_relaxed); }
 int check_launch(const char* what);  // cudaGetLastError after a launch
 
 // Brackets the kernel launches of its scope with CUDA events on `s` while

@@ -14,6 +14,7 @@
 // the eigen solver handles them in turn. Output rows are staged in shared
 // memory and leave the block as one coalesced slab.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 
@@ -701,19 +702,51 @@ constexpr uint64_t kNoAllocMaxPoints = 1u << 20;  // capacity of g_noalloc_xyz4,
 constexpr int kNoAllocMaxDevices = 64;
 
 struct NoAllocSetup {
-    std::once_flag once;
-    cudaError_t status = cudaSuccess;
+    std::mutex mu;
+    std::atomic<bool> ready{false};
     float4* xyz4 = nullptr;   // device address of g_noalloc_xyz4
     uint32_t* err = nullptr;  // device address of g_noalloc_err
 };
 NoAllocSetup g_noalloc_setup[kNoAllocMaxDevices];
 
-void noalloc_setup(NoAllocSetup& st) {
-    st.status = cudaGetSymbolAddress((void**)&st.xyz4, g_noalloc_xyz4);
-    if (st.status == cudaSuccess) st.status = cudaGetSymbolAddress((void**)&st.err, g_noalloc_err);
+// Looks the arrays' device addresses up once per device. Only success is
+// cached: a failed lookup (e.g. attempted during a stream capture) clears the
+// error it left and is retried by the next call.
+cudaError_t noalloc_setup(NoAllocSetup& st) {
+    if (st.ready.load(std::memory_order_acquire)) return cudaSuccess;
+    std::lock_guard<std::mutex> lk(st.mu);
+    if (st.ready.load(std::memory_order_relaxed)) return cudaSuccess;
+    float4* xyz4 = nullptr;
+    uint32_t* err = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&xyz4, g_noalloc_xyz4);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void**)&err, g_noalloc_err);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return e;
+    }
+    st.xyz4 = xyz4;
+    st.err = err;
+    st.ready.store(true, std::memory_order_release);
+    return cudaSuccess;
 }
 
 }  // namespace
+}  // namespace pgeof
+
+namespace pgeof {
+int noalloc_take_errors(uint32_t* bits) {
+    *bits = 0;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        (void)cudaGetLastError();
+        return PGEOF_OK;  // no device: nothing was ever recorded
+    }
+    NoAllocSetup& st = g_noalloc_setup[dev];
+    if (!st.ready.load(std::memory_order_acquire)) return PGEOF_OK;  // no call on this device yet
+    PGEOF_CUDA_TRY(cudaMemcpy(bits, st.err, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (*bits) PGEOF_CUDA_TRY(cudaMemset(st.err, 0, sizeof(uint32_t)));
+    return PGEOF_OK;
+}
 }  // namespace pgeof
 
 extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xyz, const uint32_t* nn, int64_t nnz,
@@ -736,16 +769,12 @@ extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xy
         return fail(PGEOF_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
     }
     NoAllocSetup& st = g_noalloc_setup[dev];
-    std::call_once(st.once, noalloc_setup, std::ref(st));
-    if (st.status != cudaSuccess)
-        return fail(PGEOF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(st.status));
+    e = noalloc_setup(st);
+    if (e != cudaSuccess) return fail(PGEOF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     const cudaStream_t s = (cudaStream_t)stream;
-    uint32_t* err = error_bits;
-    if (!err) {
-        // the shared word keeps the previous call's bits: clear it first
-        PGEOF_CUDA_TRY(cudaMemsetAsync(st.err, 0, sizeof(uint32_t), s));
-        err = st.err;
-    }
+    // without a caller word the bits accumulate in the library's word for this
+    // device until pgeof_take_device_errors reads and clears it
+    uint32_t* err = error_bits ? error_bits : st.err;
     if (n_points == 0) return PGEOF_OK;
     if (n_xyz > 0) {
         const unsigned blocks = (unsigned)std::min<uint64_t>(ceil_div_u((uint64_t)n_xyz, 256), 4096);

@@ -26,6 +26,8 @@ def _lib(pgeof):
     P, I64 = ctypes.c_void_p, ctypes.c_int64
     lib.pgeof_compute_features_f32.argtypes = [P, I64, P, I64, P, I64, ctypes.c_uint64, P, P]
     lib.pgeof_compute_features_f32_noalloc.argtypes = [P, I64, P, I64, P, I64, ctypes.c_uint64, P, P, P]
+    lib.pgeof_device_alloc_count.restype = ctypes.c_uint64
+    lib.pgeof_take_device_errors.argtypes = [P, ctypes.POINTER(ctypes.c_uint32)]
     return lib
 
 
@@ -59,10 +61,14 @@ def test_noalloc_matches_allocating_entry_point_on_consecutive_calls(cuda, pgeof
     ]
     for xyz, k, k_min in cases:
         t, nn, ptr = _case(torch, pgeof, xyz, k)
+        before = lib.pgeof_device_alloc_count()
         st_ref, ref = _run(lib, "pgeof_compute_features_f32", t, nn, ptr, k_min, torch)
         assert st_ref == 0
+        assert lib.pgeof_device_alloc_count() > before  # the counter sees the allocating entry point's scratch
+        before = lib.pgeof_device_alloc_count()
         st, got = _run(lib, "pgeof_compute_features_f32_noalloc", t, nn, ptr, k_min, torch)
         assert st == 0
+        assert lib.pgeof_device_alloc_count() == before, "the no-allocation entry point allocated device memory"
         assert np.isfinite(got).all()
         assert feature_close(got, ref).all()
 
@@ -79,8 +85,15 @@ def test_noalloc_reports_data_errors_and_rejects_oversize(cuda, pgeof):
     bad[5] = xyz.shape[0]  # an index past the end of xyz: flagged, never read
     st, _ = _run(lib, "pgeof_compute_features_f32_noalloc", t, bad, ptr, 1, torch, err)
     assert st == 0 and int(err.item()) & 1
-    # beyond the fixed capacity: rejected before any device work
+    # without a caller word the bits wait in the library's word for pgeof_take_device_errors
     s = torch.cuda.current_stream().cuda_stream
+    bits = ctypes.c_uint32(0)
+    assert lib.pgeof_take_device_errors(s, ctypes.byref(bits)) == 0  # drain anything earlier
+    st, _ = _run(lib, "pgeof_compute_features_f32_noalloc", t, bad, ptr, 1, torch)
+    assert st == 0
+    assert lib.pgeof_take_device_errors(s, ctypes.byref(bits)) == 0 and bits.value & 1
+    assert lib.pgeof_take_device_errors(s, ctypes.byref(bits)) == 0 and bits.value == 0  # read once, then cleared
+    # beyond the fixed capacity: rejected before any device work
     st = lib.pgeof_compute_features_f32_noalloc(t.data_ptr(), CAPACITY + 1, nn.data_ptr(), nn.shape[0],
                                                 ptr.data_ptr(), ptr.shape[0] - 1, 1, t.data_ptr(), None, s)
     assert st == 1
