@@ -63,6 +63,36 @@ def test_batch_plan_replay_on_new_data(cuda, pgeof):
     plan.close()
 
 
+def test_full_256_cloud_batch_equals_per_cloud(cuda, pgeof):
+    """The batch workload as stated: 256 clouds with sizes log-uniform in
+    [2,000, 200,000] (seed 3), each the outdoor-scene generator scaled to a
+    cube side U(5, 50) m, knn k=32 + compute_features. Every cloud's indices,
+    distances and features from the graph-captured batch plan equal its
+    per-cloud knn_search + compute_features results."""
+    torch = cuda
+    k = 32
+    sizes = log_uniform_sizes(256, 2_000, 200_000, seed=3)
+    rng = np.random.default_rng(3)
+    clouds = [torch.from_numpy(scaled_scene(int(n), seed=3000 + i, side=float(rng.uniform(5.0, 50.0)))).cuda()
+              for i, n in enumerate(sizes)]
+    assert len(clouds) == 256
+    plan = pgeof.BatchPlan(clouds, k)
+    bi, bd, bf = plan()
+    torch.cuda.synchronize()
+    off = 0
+    for j, c in enumerate(clouds):
+        n = int(c.shape[0])
+        i, d = pgeof.knn_search(c, c, k)
+        ptr = torch.arange(0, k * (n + 1), k, dtype=torch.int32, device="cuda")
+        f = pgeof.compute_features(c, i.reshape(-1), ptr)
+        assert torch.equal(bi[off:off + n].view(torch.int32), i.view(torch.int32)), f"cloud {j}: indices"
+        assert torch.equal(bd[off:off + n], d), f"cloud {j}: distances"
+        assert torch.equal(bf[off:off + n], f), f"cloud {j}: features"
+        off += n
+    assert off == plan.xyz.shape[0]
+    plan.close()
+
+
 def test_batch_errors_and_tiny_clouds(cuda, pgeof):
     torch = cuda
     a = torch.from_numpy(uniform_cube(5, seed=1)).cuda()

@@ -3,10 +3,11 @@ the oracle, through the drop-in Python API (pgeof_ext -> C ABI).
 
 Tolerance: the GPU forms the covariance with the reference's exact float
 operation order (bit-identical to the oracle's), so differences come only from
-the eigen solver: |gpu - oracle| <= 1e-4 + 1e-4 * |oracle| per feature (the
-ascending-order Scattering reaches ~1e3, hence the relative part). Normals
-are compared after sign alignment where the reference's z-flip is undefined
-(|n_z| < 1e-4).
+the eigen solver: |gpu - oracle| <= 1e-4 * max(1, |oracle|) per value (the
+ascending-order ratios reach ~1e3, hence relative above 1). Each test prints
+the per-feature maximum of that scaled error. Normals are compared after sign
+alignment where the reference's z-flip is undefined (|n_z| < 1e-4). Optimal-k
+tests print the fraction of rows whose k_opt differs from the oracle's.
 """
 
 import os
@@ -14,7 +15,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import align_normals, feature_close
+from conftest import align_normals, feature_close, feature_report
 from oracle import oracle
 from point_geometric_features_gb300.synthetic import outdoor_scene, uniform_cube
 
@@ -31,22 +32,32 @@ def _radius_csr(idx):
     return idx[idx >= 0].astype(np.uint32), np.r_[0, np.cumsum(cnt)].astype(np.uint32)
 
 
-def _assert_features(gpu, ref, frac=1.0):
+def _assert_features(gpu, ref, label=""):
     g = align_normals(gpu, ref)
+    feature_report(g, ref, label=label)
     ok = feature_close(g, ref)
-    rate = ok.all(axis=-1).mean()
-    assert rate >= frac, f"only {rate:.6f} of rows within tolerance; worst {np.abs(g - ref).max()}"
+    rate = ok.all(axis=-1).mean() if ok.size else 1.0
+    assert rate == 1.0, f"{label}: only {rate:.6f} of rows within tolerance"
+
+
+def _k_opt_mismatch(gpu, ref, label, limit=1e-3):
+    """Fraction of rows whose optimal k differs from the oracle's (printed)."""
+    diff = gpu[:, 11] != ref[:, 11]
+    rate = float(diff.mean())
+    print(f"[parity] {label} k_opt mismatch {int(diff.sum())}/{diff.size} rows = {rate:.2e}")
+    assert rate <= limit, f"{label}: k_opt differs on {rate:.2e} of rows"
+    return ~diff
 
 
 def test_golden_features(cuda, pgeof, golden):
     g = golden("features_2000_k20.npz")
     nn, nn_ptr = _csr(g["idx"])
-    _assert_features(pgeof.compute_features(g["xyz"], nn, nn_ptr), g["features"])
-    _assert_features(pgeof.compute_features_multiscale(g["xyz"], nn, nn_ptr, [5, 10, 20]), g["multiscale"])
+    _assert_features(pgeof.compute_features(g["xyz"], nn, nn_ptr), g["features"], "golden features")
+    _assert_features(pgeof.compute_features_multiscale(g["xyz"], nn, nn_ptr, [5, 10, 20]), g["multiscale"],
+                     "golden multiscale")
     opt = pgeof.compute_features_optimal(g["xyz"], nn, nn_ptr, 1, 1, 5)
-    assert (opt[:, 11] == g["optimal"][:, 11]).mean() >= 0.999
-    same = opt[:, 11] == g["optimal"][:, 11]
-    _assert_features(opt[same], g["optimal"][same])
+    same = _k_opt_mismatch(opt, g["optimal"], "golden optimal")
+    _assert_features(opt[same], g["optimal"][same], "golden optimal")
 
 
 def test_c1_uniform_10k_k20(cuda, pgeof):
@@ -56,7 +67,7 @@ def test_c1_uniform_10k_k20(cuda, pgeof):
     nn, nn_ptr = _csr(idx)
     f = pgeof.compute_features(xyz, nn, nn_ptr)
     assert f.shape == (10_000, 11) and f.dtype == np.float32
-    _assert_features(f, oracle.compute_features(xyz, nn, nn_ptr))
+    _assert_features(f, oracle.compute_features(xyz, nn, nn_ptr), "C1 10k cube k=20")
     # against the FP64 oracle, well-conditioned rows
     f64 = oracle.fp64_compute_features(xyz, nn, nn_ptr)
     gap = oracle.fp64_relative_gap(xyz[idx])
@@ -72,7 +83,7 @@ def test_scene_multiscale(cuda, pgeof):
     nn, nn_ptr = _csr(idx)
     m = pgeof.compute_features_multiscale(xyz, nn, nn_ptr, [10, 20, 50])
     assert m.shape == (50_000, 3, 11)
-    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, [10, 20, 50]))
+    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, [10, 20, 50]), "scene 50k multiscale")
     # reference self-consistency (tests/test_pgeof.py:30-46)
     single = pgeof.compute_features(xyz, nn, nn_ptr, 50)
     np.testing.assert_array_equal(m[:, 2], single)
@@ -85,11 +96,11 @@ def test_k_min_gating_and_ragged_rows(cuda, pgeof):
     for k_min in (1, 3, 10, 25):
         f = pgeof.compute_features(xyz, nn, nn_ptr, k_min)
         ref = oracle.compute_features(xyz, nn, nn_ptr, k_min)
-        _assert_features(f, ref)
+        _assert_features(f, ref, f"ragged k_min={k_min}")
         short = np.diff(nn_ptr) < k_min
         assert np.all(f[short] == 0)
     m = pgeof.compute_features_multiscale(xyz, nn, nn_ptr, [2, 5, 5, 12, 30])
-    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, [2, 5, 5, 12, 30]))
+    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, [2, 5, 5, 12, 30]), "ragged multiscale")
 
 
 def test_many_scales(cuda, pgeof):
@@ -99,7 +110,7 @@ def test_many_scales(cuda, pgeof):
     nn, nn_ptr = _csr(idx)
     scales = [2, 3, 4, 5, 6, 8, 10, 12, 15, 20, 25, 30, 40]
     m = pgeof.compute_features_multiscale(xyz, nn, nn_ptr, scales)
-    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, scales))
+    _assert_features(m, oracle.compute_features_multiscale(xyz, nn, nn_ptr, scales), "13 scales")
     empty = pgeof.compute_features_multiscale(xyz, nn, nn_ptr, [])
     assert empty.shape == (2000, 0, 11)
 
@@ -111,9 +122,8 @@ def test_optimal_radius_csr(cuda, pgeof):
     nn, nn_ptr = _radius_csr(idx)
     f = pgeof.compute_features_optimal(xyz, nn, nn_ptr, 1, 1, 10)
     ref = oracle.compute_features_optimal(xyz, nn, nn_ptr, 1, 1, 10)
-    same = f[:, 11] == ref[:, 11]
-    assert same.mean() >= 0.999, same.mean()
-    _assert_features(f[same], ref[same])
+    same = _k_opt_mismatch(f, ref, "optimal scene 40k radius")
+    _assert_features(f[same], ref[same], "optimal scene 40k radius")
     short = np.diff(nn_ptr) < 10
     assert np.all(f[short] == 0)
 
@@ -125,9 +135,8 @@ def test_optimal_steps(cuda, pgeof, k_step):
     nn, nn_ptr = _csr(idx)
     f = pgeof.compute_features_optimal(xyz, nn, nn_ptr, 3, k_step, 7)
     ref = oracle.compute_features_optimal(xyz, nn, nn_ptr, 3, k_step, 7)
-    same = f[:, 11] == ref[:, 11]
-    assert same.mean() >= 0.999
-    _assert_features(f[same], ref[same])
+    same = _k_opt_mismatch(f, ref, f"optimal k_step={k_step}")
+    _assert_features(f[same], ref[same], f"optimal k_step={k_step}")
 
 
 def test_degenerate_neighbourhoods(cuda, pgeof):
@@ -146,7 +155,7 @@ def test_degenerate_neighbourhoods(cuda, pgeof):
     nn_ptr = np.r_[0, np.cumsum(sizes)].astype(np.uint32)
     f = pgeof.compute_features(xyz, nn, nn_ptr)
     ref = oracle.compute_features(xyz, nn, nn_ptr)
-    _assert_features(f, ref)
+    _assert_features(f, ref, "degenerate neighbourhoods")
 
 
 def test_csr_validation(cuda, pgeof):
@@ -181,7 +190,7 @@ def test_descending_order_switch(cuda, pgeof):
     finally:
         pgeof.set_eig_order("ascending")
     ref = oracle.compute_features(xyz, nn, nn_ptr, order=oracle.EIG_DESCENDING)
-    _assert_features(f, ref)
+    _assert_features(f, ref, "descending order")
     ground = np.abs(xyz[:, 2]) < 0.03
     assert np.median(f[ground, 6]) > 0.99  # normals of the ground plane point up
 
@@ -199,7 +208,7 @@ def test_full_size_multiscale_properties(cuda, pgeof):
     sub_nn = idx[rows].reshape(-1).astype(np.uint32)
     sub_ptr = (np.arange(rows.size + 1) * 50).astype(np.uint32)
     ref = oracle.compute_features_multiscale(xyz, sub_nn, sub_ptr, [10, 20, 50])
-    _assert_features(m[rows], ref)
+    _assert_features(m[rows], ref, "1M scene multiscale, 5000-row sample")
 
 
 @pytest.mark.parametrize("k", [8, 50])
