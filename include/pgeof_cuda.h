@@ -237,8 +237,11 @@ int pgeof_batch_knn_features_f32(const float* xyz, const int64_t* offsets, int64
                                  uint32_t* indices, float* sqr_dist, float* features, pgeof_stream_t stream);
 
 /* The same pipeline captured once into a CUDA graph for a fixed batch shape
- * and fixed device buffers: create (tunes the grid cell size on the given
- * data, synchronises `stream`), then launch any number of times after
+ * and fixed device buffers: create (tunes the speed parameters on the given
+ * data -- the grid cell occupancy factor and the queries per search work
+ * item -- or reuses those of an earlier plan of the same shape class: device,
+ * knn and the log2 buckets of the point count, mean cloud size and cloud
+ * count; synchronises `stream`), then launch any number of times after
  * refilling xyz in place. No reference counterpart (the reference has no
  * batch API). */
 typedef struct pgeof_batch_plan_s* pgeof_batch_plan;
@@ -246,6 +249,12 @@ int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_
                             uint32_t* indices, float* sqr_dist, float* features, pgeof_stream_t stream,
                             pgeof_batch_plan* out);
 int pgeof_batch_plan_launch(pgeof_batch_plan plan, pgeof_stream_t stream);
+/* The parameters a plan runs with: cell occupancy factor (times the default
+ * knn / 3.5 points per cell), queries per search work item, the pipeline time
+ * with them and with the defaults (1.0, 16) at tuning, and whether they came
+ * from the shape-class cache. Any output pointer may be NULL. */
+int pgeof_batch_plan_info(pgeof_batch_plan plan, float* cell_factor, uint32_t* queries_per_item, float* tuned_ms,
+                          float* default_ms, int* from_cache);
 int pgeof_batch_plan_destroy(pgeof_batch_plan plan);
 
 /* ------------------------------------------------ request server */

@@ -433,6 +433,15 @@ class BatchPlan:
         _ext._batch_plan_launch(self._h, _stream_handle(stream))
         return self.indices, self.sqr_dist, self.features
 
+    def info(self):
+        """The speed parameters the plan runs with (chosen by the autotuner at
+        creation, or reused from an earlier plan of the same shape class) and
+        the pipeline times measured with them and with the defaults."""
+        cell, chunk, tuned, dflt, cached = _ext._batch_plan_info(self._h)
+        return {"cell_factor": round(float(cell), 3), "queries_per_work_item": int(chunk),
+                "warps_per_query": 1, "tuned_ms": round(float(tuned), 4), "default_ms": round(float(dflt), 4),
+                "from_cache": bool(cached)}
+
     def close(self):
         if getattr(self, "_h", 0):
             _ext._batch_plan_destroy(self._h)

@@ -13,6 +13,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "kernels.cuh"
@@ -96,6 +99,9 @@ __device__ void cloud_params(const float* mn, const float* mx, double h, uint64_
             g.oz = mn[2];
             g.h = (float)h;
             g.inv_h = (float)(1.0 / h);
+            g.hx = g.h;
+            g.inv_hx = g.inv_h;
+            g.xsub = 1;
             g.gx = d[0];
             g.gy = d[1];
             g.gz = d[2];
@@ -150,7 +156,7 @@ __global__ void batch_params_kernel(const uint32_t* __restrict__ box, const uint
 }
 
 __device__ __forceinline__ uint32_t local_cell(const GridParams& g, float x, float y, float z) {
-    const float fx = (x - g.ox) * g.inv_h, fy = (y - g.oy) * g.inv_h, fz = (z - g.oz) * g.inv_h;
+    const float fx = (x - g.ox) * g.inv_hx, fy = (y - g.oy) * g.inv_h, fz = (z - g.oz) * g.inv_h;
     const int cx = (int)floorf(fminf(fmaxf(fx, 0.0f), (float)(g.gx - 1)));
     const int cy = (int)floorf(fminf(fmaxf(fy, 0.0f), (float)(g.gy - 1)));
     const int cz = (int)floorf(fminf(fmaxf(fz, 0.0f), (float)(g.gz - 1)));
@@ -295,14 +301,23 @@ int workspace_init(BatchWorkspace& w, const int64_t* offsets, int64_t n_clouds, 
 // exclusive scan of w.counts[0..max_cells) into w.cell_start (three passes)
 int batch_scan(BatchWorkspace& w, cudaStream_t s);
 
+// Speed parameters of the pipeline (results never depend on them): the grid
+// cell occupancy target as a factor of the default k / 3.5 points per cell
+// (each cloud's edge is still fitted to its own density), and the consecutive
+// queries of one search work item.
+struct BatchTune {
+    float cell = 1.0f;
+    uint32_t chunk = 16;
+};
+
 // The whole pipeline: enqueue only (no host synchronisation, no allocation).
-int run_pipeline(BatchWorkspace& w, const float* xyz, uint32_t* idx, float* d2, float* features, float tune,
-                 cudaStream_t s) {
+int run_pipeline(BatchWorkspace& w, const float* xyz, uint32_t* idx, float* d2, float* features,
+                 const BatchTune& tune, cudaStream_t s) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     const int nc = w.n_clouds;
     const uint64_t n = w.n;
-    const float target = std::min(48.0f, std::max(2.0f, (float)w.k / 3.5f * tune));
+    const float target = std::min(48.0f, std::max(2.0f, (float)w.k / 3.5f * tune.cell));
     // 1. bounding boxes
     box_init_kernel<<<blocks_for(6 * (uint64_t)nc, 256, di->sm_count), 256, 0, s>>>(w.box, nc);
     {
@@ -339,7 +354,7 @@ int run_pipeline(BatchWorkspace& w, const float* xyz, uint32_t* idx, float* d2, 
     ct.cell_base = w.cell_base;
     ct.off = w.off;
     ct.n = nc;
-    PGEOF_TRY(launch_search_batch(ct, w.cell_start, w.pts, n, w.k, idx, d2, w.words, w.words + 8, s));
+    PGEOF_TRY(launch_search_batch(ct, w.cell_start, w.pts, n, w.k, idx, d2, w.words, w.words + 8, s, tune.chunk));
     // 5. features from the kNN rows (CSR with nn_ptr = k * row)
     if (features) {
         PGEOF_TRY(pad_xyz(xyz, n, w.xyz4, s));
@@ -365,8 +380,70 @@ struct BatchPlan {
     BatchWorkspace w;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    float tune = 1.0f;
+    BatchTune tune;
+    float tuned_ms = 0.0f;    // pipeline time with `tune` at creation
+    float default_ms = 0.0f;  // ... and with the default parameters
+    int from_cache = 0;       // `tune` came from an earlier plan of the same shape class
 };
+
+// Tuned parameters by batch shape class: (device, k, log2 of the point count,
+// log2 of the mean cloud size, log2 of the cloud count). A plan of a class
+// seen before reuses its parameters without re-tuning.
+using TuneKey = std::tuple<int, uint32_t, int, int, int>;
+struct TuneEntry {
+    BatchTune tune;
+    float tuned_ms, default_ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune_cache;
+
+int log2_bucket(double v) { return v >= 1.0 ? (int)std::floor(std::log2(v)) : 0; }
+
+// Times every candidate (cell factor x work-item size) twice on the plan's
+// own data and keeps the fastest second run.
+int autotune(BatchPlan* plan, const float* xyz, uint32_t* indices, float* sqr_dist, float* features, cudaStream_t s) {
+    static const float kCells[3] = {0.6f, 1.0f, 1.6f};
+    static const uint32_t kChunks[3] = {8, 16, 32};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    PGEOF_CUDA_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return fail(PGEOF_ERR_CUDA, "batch autotune: event");
+    }
+    int st = PGEOF_OK;
+    float best = 1e30f;
+    for (int rep = 0; rep < 2 && st == PGEOF_OK; ++rep) {
+        for (float c : kCells) {
+            for (uint32_t q : kChunks) {
+                BatchTune t;
+                t.cell = c;
+                t.chunk = q;
+                cudaEventRecord(e0, s);
+                st = run_pipeline(plan->w, xyz, indices, sqr_dist, features, t, s);
+                cudaEventRecord(e1, s);
+                if (st != PGEOF_OK) break;
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    st = fail(PGEOF_ERR_CUDA, "batch autotune");
+                    break;
+                }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep == 1) {
+                    if (ms < best) {
+                        best = ms;
+                        plan->tune = t;
+                        plan->tuned_ms = ms;
+                    }
+                    if (c == 1.0f && q == 16) plan->default_ms = ms;
+                }
+            }
+            if (st != PGEOF_OK) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return st;
+}
 
 }  // namespace pgeof
 
@@ -399,7 +476,7 @@ int pgeof_batch_knn_features_f32(const float* xyz, const int64_t* offsets, int64
     const cudaStream_t s = (cudaStream_t)stream;
     BatchWorkspace w;
     PGEOF_TRY(workspace_init(w, offsets, n_clouds, knn, true, s));
-    const int st = run_pipeline(w, xyz, indices, sqr_dist, features, 1.0f, s);
+    const int st = run_pipeline(w, xyz, indices, sqr_dist, features, BatchTune{}, s);
     scratch_free(w.base, s);
     return st;
 }
@@ -414,33 +491,32 @@ int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_
     const cudaStream_t s = (cudaStream_t)stream;
     BatchPlan* plan = new BatchPlan();
     int st = workspace_init(plan->w, offsets, n_clouds, knn, false, s);
-    // autotune the cell-occupancy target on this batch (results never depend on it)
+    // tune the speed parameters on this batch, or reuse those of its shape class
     if (st == PGEOF_OK) {
-        const float tunes[3] = {0.6f, 1.0f, 1.6f};
-        float best_ms = 1e30f;
-        cudaEvent_t e0, e1;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        for (int rep = 0; rep < 2 && st == PGEOF_OK; ++rep) {
-            for (float t : tunes) {
-                cudaEventRecord(e0, s);
-                st = run_pipeline(plan->w, xyz, indices, sqr_dist, features, t, s);
-                cudaEventRecord(e1, s);
-                if (st != PGEOF_OK) break;
-                if (cudaEventSynchronize(e1) != cudaSuccess) {
-                    st = fail(PGEOF_ERR_CUDA, "batch autotune");
-                    break;
-                }
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (rep == 1 && ms < best_ms) {
-                    best_ms = ms;
-                    plan->tune = t;
-                }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const double total = (double)offsets[n_clouds];
+        const TuneKey key{dev, knn, log2_bucket(total), log2_bucket(total / (double)n_clouds),
+                          log2_bucket((double)n_clouds)};
+        bool cached = false;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            const auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end()) {
+                plan->tune = it->second.tune;
+                plan->tuned_ms = it->second.tuned_ms;
+                plan->default_ms = it->second.default_ms;
+                plan->from_cache = 1;
+                cached = true;
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        if (!cached) {
+            st = autotune(plan, xyz, indices, sqr_dist, features, s);
+            if (st == PGEOF_OK) {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                g_tune_cache[key] = TuneEntry{plan->tune, plan->tuned_ms, plan->default_ms};
+            }
+        }
     }
     // capture the tuned pipeline once
     if (st == PGEOF_OK) {
@@ -475,6 +551,18 @@ int pgeof_batch_plan_launch(pgeof_batch_plan handle, pgeof_stream_t stream) {
     if (!plan || !plan->exec) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid plan");
     PGEOF_CUDA_TRY(cudaGraphLaunch(plan->exec, (cudaStream_t)stream));
     count_launch(1);
+    return PGEOF_OK;
+}
+
+int pgeof_batch_plan_info(pgeof_batch_plan handle, float* cell_factor, uint32_t* queries_per_item, float* tuned_ms,
+                          float* default_ms, int* from_cache) {
+    const BatchPlan* plan = reinterpret_cast<const BatchPlan*>(handle);
+    if (!plan) return fail(PGEOF_ERR_INVALID_ARGUMENT, "invalid plan");
+    if (cell_factor) *cell_factor = plan->tune.cell;
+    if (queries_per_item) *queries_per_item = plan->tune.chunk;
+    if (tuned_ms) *tuned_ms = plan->tuned_ms;
+    if (default_ms) *default_ms = plan->default_ms;
+    if (from_cache) *from_cache = plan->from_cache;
     return PGEOF_OK;
 }
 

@@ -253,23 +253,40 @@ int features_impl(const float* xyz, uint64_t n_xyz, const uint32_t* nn, uint64_t
                            (int)n_scales, out, nullptr, s);
 }
 
-// include/pgeof.hpp:325-375 on an existing grid of xyz: radius table (the
-// nearest max_knn inside the radius, uncapped counts), then PCA + features.
+// include/pgeof.hpp:325-375 on an existing grid of xyz: the radius search
+// hands each query's nearest min(found, max_knn) straight to PCA and the
+// selected features (no neighbour table). Feature lists longer than one
+// launch's share run the search once per share of ids.
 template <typename T>
 int selected_on_grid(const GridIndex<T>& grid, const T* xyz, uint64_t n, T radius, uint32_t max_knn,
                      const int32_t* ids, int64_t n_ids, T* out, cudaStream_t s) {
+    if (n >= 0xffffffffull) return fail(PGEOF_ERR_INVALID_ARGUMENT, "compute_features_selected: too many points");
     const uint32_t k_search = std::max<uint32_t>(max_knn, 1u);
-    Scratch nbr, found;
-    PGEOF_TRY(nbr.alloc(n * (uint64_t)k_search * sizeof(int32_t), s));
-    PGEOF_TRY(found.alloc(n * sizeof(uint32_t), s));
+    SelSpec<T> sp;
+    Scratch xyz4;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // one 16-byte gather per neighbour instead of three 4-byte ones
+        PGEOF_TRY(xyz4.alloc(n * sizeof(float4), s));
+        PGEOF_TRY(pad_xyz(reinterpret_cast<const float*>(xyz), n, xyz4.as<float4>(), s));
+        sp.xyz4 = xyz4.as<float4>();
+    } else {
+        sp.xyz = xyz;
+    }
+    sp.out = out;
+    sp.max_knn = max_knn;
+    sp.out_stride = (uint32_t)n_ids;
+    sp.order = eig_order();
+    sp.ring = sel_ring_slots(k_search);
     SearchOut<T> so;
-    so.indices = nbr.p;
-    so.sqr_dist = nullptr;
-    so.found = found.as<uint32_t>();
     so.radius_fill_last = false;
-    PGEOF_TRY(launch_search<T>(grid, grid.pts, grid.cell_start, n, MODE_RADIUS, k_search, radius, so, s));
-    return launch_selected_pca<T>(xyz, n, nbr.as<int32_t>(), found.as<uint32_t>(), max_knn, ids, (int)n_ids, out,
-                                  s);
+    so.sel = &sp;
+    for (int64_t off = 0; off < n_ids; off += kSelMaxIds) {
+        sp.id_offset = (uint32_t)off;
+        sp.n_ids = (int)std::min<int64_t>(kSelMaxIds, n_ids - off);
+        for (int t = 0; t < sp.n_ids; ++t) sp.ids[t] = ids[off + t];
+        PGEOF_TRY(launch_search<T>(grid, grid.pts, grid.cell_start, n, MODE_RADIUS, k_search, radius, so, s));
+    }
+    return PGEOF_OK;
 }
 
 template <typename T>
@@ -428,6 +445,15 @@ struct OccEntry {
 };
 std::mutex g_occ_mu;
 std::vector<OccEntry> g_occ;
+// Largest dynamic shared memory limit set on each (device, kernel): the limit
+// is only ever raised, so a launch whose size was cached earlier stays valid
+// after launches of the same kernel with other sizes.
+struct SmemLimit {
+    int device;
+    const void* kernel;
+    int limit;
+};
+std::vector<SmemLimit> g_smem_limit;
 
 // Cache of page-locked host blocks behind pgeof_host_alloc / pgeof_host_free.
 struct HostPool {
@@ -456,20 +482,28 @@ size_t host_pool_cap(HostPool& hp) {
 int pgeof::kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* per_sm) {
     int dev = 0;
     PGEOF_CUDA_TRY(cudaGetDevice(&dev));
-    {
-        std::lock_guard<std::mutex> lk(g_occ_mu);
-        for (const OccEntry& e : g_occ)
-            if (e.device == dev && e.kernel == kernel && e.threads == threads && e.smem == smem) {
-                *per_sm = e.per_sm;
-                return PGEOF_OK;
-            }
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    for (const OccEntry& e : g_occ)
+        if (e.device == dev && e.kernel == kernel && e.threads == threads && e.smem == smem) {
+            *per_sm = e.per_sm;
+            return PGEOF_OK;
+        }
+    if (smem > 48 * 1024) {
+        SmemLimit* lim = nullptr;
+        for (SmemLimit& l : g_smem_limit)
+            if (l.device == dev && l.kernel == kernel) lim = &l;
+        if (!lim) {
+            g_smem_limit.push_back(SmemLimit{dev, kernel, 48 * 1024});
+            lim = &g_smem_limit.back();
+        }
+        if (smem > lim->limit) {
+            PGEOF_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            lim->limit = smem;
+        }
     }
-    if (smem > 48 * 1024)
-        PGEOF_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int n = 0;
     PGEOF_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem));
     n = std::max(n, 1);
-    std::lock_guard<std::mutex> lk(g_occ_mu);
     g_occ.push_back(OccEntry{dev, kernel, threads, smem, n});
     *per_sm = n;
     return PGEOF_OK;

@@ -15,6 +15,7 @@
 // edge is found by two trial histograms and a power-law fit of their exponent.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -58,7 +59,7 @@ __global__ void bbox_kernel(const T* __restrict__ xyz, uint64_t n, uint32_t* out
 
 template <typename T>
 __device__ __forceinline__ uint32_t cell_of(const GridParams& g, T x, T y, T z) {
-    const float fx = ((float)x - g.ox) * g.inv_h;
+    const float fx = ((float)x - g.ox) * g.inv_hx;
     const float fy = ((float)y - g.oy) * g.inv_h;
     const float fz = ((float)z - g.oz) * g.inv_h;
     const int cx = (int)floorf(fminf(fmaxf(fx, 0.0f), (float)(g.gx - 1)));
@@ -248,13 +249,15 @@ void edge_cache_put(const EdgeKey& k, double h) {
     g_edge_n = std::min(g_edge_n + 1, 16);
 }
 
-// Grid dimensions for edge h, or false when it would exceed `cap` cells.
-static bool make_params(const HostBox& b, double h, uint64_t cap, GridParams& g) {
+// Grid dimensions for edge h (x edge h / xsub), or false when it would
+// exceed `cap` cells.
+static bool make_params(const HostBox& b, double h, uint64_t cap, GridParams& g, int xsub = 1) {
     uint64_t G = 1;
     int d[3];
+    const double hx = h / xsub;
     for (int a = 0; a < 3; ++a) {
         const double ext = (double)b.mx[a] - (double)b.mn[a];
-        const double cells = std::floor(ext / h) + 1.0;
+        const double cells = std::floor(ext / (a == 0 ? hx : h)) + 1.0;
         if (cells > 2.0e9) return false;
         d[a] = (int)cells;
         G *= (uint64_t)d[a];
@@ -265,6 +268,9 @@ static bool make_params(const HostBox& b, double h, uint64_t cap, GridParams& g)
     g.oz = b.mn[2];
     g.h = (float)h;
     g.inv_h = (float)(1.0 / h);
+    g.hx = (float)hx;
+    g.inv_hx = (float)(1.0 / hx);
+    g.xsub = xsub;
     g.gx = d[0];
     g.gy = d[1];
     g.gz = d[2];
@@ -411,8 +417,23 @@ int build_grid(const T* xyz, uint64_t n, uint32_t k_target, float h_min, float h
         }
     }
     edge_cache_put(key, h);
+    // the final grid splits cells along x (see GridParams) while the cell
+    // table stays within 8 entries per point
     GridParams g;
     make_params(b, h, cap, g);
+    static const int xsub_max = [] {
+        const char* e = getenv("PGEOF_GRID_XSUB");
+        const int v = e ? atoi(e) : 4;
+        return v < 1 ? 1 : (v > 16 ? 16 : v);
+    }();
+    const uint64_t cap_fine = std::max<uint64_t>(8 * n, 1u << 16);
+    for (int xs = xsub_max; xs > 1; xs /= 2) {
+        GridParams gf;
+        if (make_params(b, h, cap_fine, gf, xs)) {
+            g = gf;
+            break;
+        }
+    }
     out.g = g;
     // 3. counting sort into cells
     PGEOF_TRY(out.cell_mem.alloc(((size_t)g.n_cells + 1) * sizeof(uint32_t), s));

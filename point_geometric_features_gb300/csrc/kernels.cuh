@@ -39,13 +39,18 @@ int launch_optimal(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint6
 // ----------------------------------------------------------- grid index
 // Uniform grid over the bounding box. Cells are numbered x-fastest
 // (id = (cz * gy + cy) * gx + cx); points are counting-sorted by cell so every
-// cell, and every run of cells along x, is one contiguous range.
+// cell, and every run of cells along x, is one contiguous range. Cells may be
+// split `xsub` times along x: a search still reads one contiguous run per row
+// of cells (fixed y, z), so the finer x edge only trims the ends of each run
+// closer to the query's sphere, at no cost in rows.
 struct GridParams {
-    float ox, oy, oz;  // origin (bounding-box minimum)
-    float h, inv_h;    // cell edge and its inverse
-    int gx, gy, gz;    // cells per axis
-    uint32_t n_cells;  // gx * gy * gz
-    float margin;      // slack added to every cell-distance bound
+    float ox, oy, oz;    // origin (bounding-box minimum)
+    float h, inv_h;      // cell edge along y and z, and its inverse
+    float hx, inv_hx;    // cell edge along x (h / xsub), and its inverse
+    int xsub;            // x cells per y/z edge
+    int gx, gy, gz;      // cells per axis
+    uint32_t n_cells;    // gx * gy * gz
+    float margin;        // slack added to every cell-distance bound
 };
 
 // Min / max of three coordinates over the block (blockDim.x a multiple of 32,
@@ -142,6 +147,35 @@ __device__ __forceinline__ int cloud_of(const CloudTable& ct, uint64_t pos) {
 // ----------------------------------------------------------- neighbour search
 enum SearchMode { MODE_KNN = 0, MODE_RADIUS = 1 };
 
+// compute_features_selected fused into the radius search
+// (include/pgeof.hpp:325-375): each query's nearest min(found, max_knn)
+// neighbours go from the search's selection straight to PCA and the selected
+// features; no neighbour table is written.
+constexpr int kSelMaxIds = 32;  // feature ids per launch
+template <typename T>
+struct SelSpec {
+    const float4* xyz4 = nullptr;  // float: the cloud padded to 16-byte rows, original order
+    const T* xyz = nullptr;        // double: the cloud, (n, 3), original order
+    T* out = nullptr;              // (n, out_stride)
+    uint32_t max_knn = 0;
+    uint32_t out_stride = 0;       // values per output row
+    uint32_t id_offset = 0;        // first output column of this launch
+    int n_ids = 0;
+    int ids[kSelMaxIds] = {};
+    int order = 0;
+    int ring = 1;                  // queries a warp gathers before its lanes solve them together
+};
+// Queries a warp parks before solving them one per lane: up to 32 while the
+// parked neighbour lists fit ~4 KB of shared memory per warp.
+__host__ __device__ inline int sel_ring_slots(uint32_t max_knn) {
+    const uint32_t r = 1024u / (max_knn > 0 ? max_knn : 1u);
+    return (int)(r < 1 ? 1 : (r > 32 ? 32 : r));
+}
+__host__ __device__ inline size_t sel_ring_bytes(uint32_t max_knn, int ring) {
+    const size_t words = (size_t)(max_knn > 0 ? max_knn : 1) * (ring + 1) + 2 * (size_t)ring;
+    return (words * sizeof(uint32_t) + 15) / 16 * 16;
+}
+
 template <typename T>
 struct SearchOut {
     void* indices = nullptr;          // uint32 (knn) or int32 (radius), (m, k)
@@ -149,6 +183,7 @@ struct SearchOut {
     uint32_t* found = nullptr;        // optional: uncapped count inside the radius
     bool radius_fill_last = true;     // nanoflann RKNN: radius^2 in the last slot of short rows
     bool rows_in_query_order = false; // row q holds queries[q] (cell order), not queries[q].idx
+    const SelSpec<T>* sel = nullptr;  // radius mode: selected features instead of the table
 };
 
 // `queries` are in `grid`'s cell order; `qstart` (n_cells + 1) gives each
@@ -161,9 +196,10 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
 // cell) order with cloud-local indices, `cell_start` the shared cell table;
 // output rows are global (off[c] + local index), neighbour indices local.
 // `work` points to 8 zeroed words and `ovf` to n_points words of device scratch.
+// `chunk`: consecutive queries per work item of the search (speed only).
 int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const SPoint<float>* pts, uint64_t n_points,
                         uint32_t k, uint32_t* indices, float* sqr_dist, uint32_t* work, uint32_t* ovf,
-                        cudaStream_t s);
+                        cudaStream_t s, uint32_t chunk = 16);
 
 // Exclusive scan of G counts into out[0..G] (out[G] = total) with caller-owned
 // partials (ceil(G / 1024) words).
@@ -189,9 +225,5 @@ int resident_cloud_build(const float* xyz, uint64_t n, float radius_hint, uint32
 int host_selected_resident(const ResidentCloud& c, float radius, uint32_t max_knn, const int32_t* ids,
                            int64_t n_ids, float* features);
 
-// PCA + selected features from a radius-search neighbour table (selected path).
-template <typename T>
-int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint32_t* found, uint32_t max_knn,
-                        const int32_t* ids, int n_ids, T* out, cudaStream_t s);
 
 }  // namespace pgeof

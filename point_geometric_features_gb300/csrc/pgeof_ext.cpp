@@ -415,6 +415,13 @@ PYBIND11_MODULE(pgeof_ext, m) {
         py::gil_scoped_release nogil;
         check(pgeof_batch_plan_launch(reinterpret_cast<pgeof_batch_plan>(plan), P<void>(stream)));
     });
+    m.def("_batch_plan_info", [](uintptr_t plan) {
+        float cell = 0.0f, tuned = 0.0f, dflt = 0.0f;
+        uint32_t chunk = 0;
+        int cached = 0;
+        check(pgeof_batch_plan_info(reinterpret_cast<pgeof_batch_plan>(plan), &cell, &chunk, &tuned, &dflt, &cached));
+        return py::make_tuple(cell, chunk, tuned, dflt, cached != 0);
+    });
     m.def("_batch_plan_destroy", [](uintptr_t plan) {
         check(pgeof_batch_plan_destroy(reinterpret_cast<pgeof_batch_plan>(plan)));
     });

@@ -28,6 +28,13 @@
 //    then passes over the cells within that bound refine a window of bins (first
 //    on d^2, then on the index when distances tie exactly) until the survivors
 //    fit the buffer.
+//
+// compute_features_selected runs inside the radius search (SEL instantiations):
+// instead of writing a query's row, a warp parks its sorted neighbour indices
+// in shared memory; once `ring` queries are parked, each lane takes one of
+// them through the reference's two-pass covariance, the eigen solver and the
+// selected features (thread-level work, done by the whole warp at once). No
+// neighbour table reaches global memory.
 #include <algorithm>
 
 #include "eig3.cuh"
@@ -116,6 +123,7 @@ struct SearchArgs {
     int fill_last;
     int rows_sorted;  // output row = position in `queries`
     uint32_t* err;
+    SelSpec<T> sel;   // SEL instantiations
 };
 
 struct Box {
@@ -174,8 +182,8 @@ __device__ __forceinline__ void visit_box(const GridView<T>& gv, uint32_t* run_s
                     keep = false;
                 } else {
                     const float bxr = sqrtf(Rf2 - dyz2) + g.margin;
-                    xa = max(xa, cell_floor((qf0 - bxr - g.ox) * g.inv_h, g.gx));
-                    xb = min(xb, cell_floor((qf0 + bxr - g.ox) * g.inv_h, g.gx));
+                    xa = max(xa, cell_floor((qf0 - bxr - g.ox) * g.inv_hx, g.gx));
+                    xb = min(xb, cell_floor((qf0 + bxr - g.ox) * g.inv_hx, g.gx));
                 }
             }
             if (keep && xa <= xb) {
@@ -238,9 +246,10 @@ __device__ __forceinline__ void query_cell(const GridParams& g, float x, float y
     const float v[3] = {x, y, z};
     const float o[3] = {g.ox, g.oy, g.oz};
     const int gd[3] = {g.gx, g.gy, g.gz};
+    const float inv[3] = {g.inv_hx, g.inv_h, g.inv_h};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const float c = (v[d] - o[d]) * g.inv_h;
+        const float c = (v[d] - o[d]) * inv[d];
         cq[d] = (int)floorf(fminf(fmaxf(c, 0.0f), (float)(gd[d] - 1)));
     }
 }
@@ -262,8 +271,9 @@ __device__ __forceinline__ T pilot_tau2(const GridView<T>& gv, uint32_t* hist32,
         bool full = true;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            bx.lo[d] = max(0, cq[d] - r);
-            bx.hi[d] = min(gd[d] - 1, cq[d] + r);
+            const int rd = d == 0 ? r * g.xsub + (g.xsub - 1) / 2 : r;  // the same extent in metres on every axis
+            bx.lo[d] = max(0, cq[d] - rd);
+            bx.hi[d] = min(gd[d] - 1, cq[d] + rd);
             full = full && bx.lo[d] == 0 && bx.hi[d] == gd[d] - 1;
         }
         const int ny = bx.hi[1] - bx.lo[1] + 1, nz = bx.hi[2] - bx.lo[2] + 1;
@@ -277,9 +287,10 @@ __device__ __forceinline__ T pilot_tau2(const GridView<T>& gv, uint32_t* hist32,
         if (cnt >= k || full) break;
     }
     float F2 = 0.0f;
+    const float hd[3] = {g.hx, g.h, g.h};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const float lo = go[d] + (float)bx.lo[d] * g.h, hi = go[d] + (float)(bx.hi[d] + 1) * g.h;
+        const float lo = go[d] + (float)bx.lo[d] * hd[d], hi = go[d] + (float)(bx.hi[d] + 1) * hd[d];
         const float far = fmaxf((float)q[d] - lo, hi - (float)q[d]) + g.margin;
         F2 += far * far;
     }
@@ -316,11 +327,12 @@ __device__ __forceinline__ Box region_box(const GridParams& g, float qx, float q
     const float v[3] = {qx, qy, qz};
     const float o[3] = {g.ox, g.oy, g.oz};
     const int gd[3] = {g.gx, g.gy, g.gz};
+    const float inv[3] = {g.inv_hx, g.inv_h, g.inv_h};
     Box rb;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        rb.lo[d] = max(0, cell_floor((v[d] - tf - o[d]) * g.inv_h, gd[d]));
-        rb.hi[d] = min(gd[d] - 1, cell_floor((v[d] + tf - o[d]) * g.inv_h, gd[d]));
+        rb.lo[d] = max(0, cell_floor((v[d] - tf - o[d]) * inv[d], gd[d]));
+        rb.hi[d] = min(gd[d] - 1, cell_floor((v[d] + tf - o[d]) * inv[d], gd[d]));
     }
     return rb;
 }
@@ -405,8 +417,135 @@ __device__ __forceinline__ void emit_row(int mode, uint32_t k, uint32_t n_sel, u
     }
 }
 
-// ------------------------------------------------------------------ general
+// ------------------------------------------------------------------ fused selected
 template <typename T>
+__device__ __forceinline__ void solve(const Cov<T>& c, int order, Pca<T>& p);
+template <>
+__device__ __forceinline__ void solve<float>(const Cov<float>& c, int order, Pca<float>& p) {
+    bool res;
+    pca_solve_f32(c, order, p, res);
+}
+template <>
+__device__ __forceinline__ void solve<double>(const Cov<double>& c, int order, Pca<double>& p) {
+    pca_solve_f64<double>(c, order, &p);
+}
+
+// A warp's parking area for selected-feature queries: the sorted neighbour
+// indices of up to `ring` queries, stored [j][slot] with rows of ring + 1 words
+// (writing one query's column and reading one lane's column are both free of
+// bank conflicts), plus their uncapped counts and output rows.
+struct SelRing {
+    uint32_t* idx;    // [max(max_knn, 1)][ring + 1]
+    uint32_t* found;  // [ring]
+    uint32_t* row;    // [ring]
+    int n;            // parked queries (warp-uniform)
+};
+
+__device__ __forceinline__ SelRing sel_ring_at(unsigned char* base, uint32_t max_knn, int ring) {
+    SelRing r;
+    r.idx = reinterpret_cast<uint32_t*>(base);
+    r.found = r.idx + (size_t)(max_knn > 0 ? max_knn : 1) * (ring + 1);
+    r.row = r.found + ring;
+    r.n = 0;
+    return r;
+}
+
+__device__ __forceinline__ void sel_point(const SelSpec<float>& sp, uint32_t id, float& x, float& y, float& z) {
+    const float4 p = __ldg(sp.xyz4 + id);
+    x = p.x;
+    y = p.y;
+    z = p.z;
+}
+__device__ __forceinline__ void sel_point(const SelSpec<double>& sp, uint32_t id, double& x, double& y, double& z) {
+    x = __ldg(sp.xyz + 3 * (uint64_t)id);
+    y = __ldg(sp.xyz + 3 * (uint64_t)id + 1);
+    z = __ldg(sp.xyz + 3 * (uint64_t)id + 2);
+}
+
+// include/pgeof.hpp:354-369 for one parked query, on one lane: fewer than 2
+// points in the radius -> zeros; otherwise the PCA of the nearest
+// min(found, max_knn) in (distance, index) order -- two sequential sweeps, the
+// operation order of include/pca.hpp:75-76 -- and the selected features.
+// `idx` is the query's column of the parking area (entries `stride` apart).
+template <typename T>
+__device__ __noinline__ void sel_solve(const SelSpec<T>& sp, const uint32_t* idx, int stride, uint32_t found,
+                                       uint32_t row) {
+    using O = XOps<T>;
+    T* o = sp.out + (uint64_t)row * sp.out_stride + sp.id_offset;
+    if (found < 2) {
+        for (int t = 0; t < sp.n_ids; ++t) o[t] = T(0);
+        return;
+    }
+    const uint32_t k = min(found, sp.max_knn);
+    T sx = 0, sy = 0, sz = 0;
+#pragma unroll 4
+    for (uint32_t j = 0; j < k; ++j) {
+        T x, y, z;
+        sel_point(sp, idx[(size_t)j * stride], x, y, z);
+        sx = O::add(sx, x);
+        sy = O::add(sy, y);
+        sz = O::add(sz, z);
+    }
+    const T kk = (T)k;
+    const T mx = O::div(sx, kk), my = O::div(sy, kk), mz = O::div(sz, kk);
+    T xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0;
+#pragma unroll 4
+    for (uint32_t j = 0; j < k; ++j) {
+        T x, y, z;
+        sel_point(sp, idx[(size_t)j * stride], x, y, z);
+        const T dx = O::sub(x, mx), dy = O::sub(y, my), dz = O::sub(z, mz);
+        xx = O::add(xx, O::mul(dx, dx));
+        xy = O::add(xy, O::mul(dx, dy));
+        xz = O::add(xz, O::mul(dx, dz));
+        yy = O::add(yy, O::mul(dy, dy));
+        yz = O::add(yz, O::mul(dy, dz));
+        zz = O::add(zz, O::mul(dz, dz));
+    }
+    Cov<T> c;
+    c.xx = O::div(xx, kk);
+    c.xy = O::div(xy, kk);
+    c.xz = O::div(xz, kk);
+    c.yy = O::div(yy, kk);
+    c.yz = O::div(yz, kk);
+    c.zz = O::div(zz, kk);
+    Pca<T> p;
+    solve<T>(c, sp.order, p);
+    for (int t = 0; t < sp.n_ids; ++t) {
+        T v = T(0);
+        if (!selected_feature<T>(p, sp.ids[t], v)) v = T(0);
+        o[t] = v;
+    }
+}
+
+// Every lane takes one parked query (warp-wide call).
+template <typename T>
+__device__ __forceinline__ void sel_flush(const SelSpec<T>& sp, SelRing& rg) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < rg.n) sel_solve<T>(sp, rg.idx + lane, sp.ring + 1, rg.found[lane], rg.row[lane]);
+    __syncwarp();
+    rg.n = 0;
+}
+
+// Park one query (warp-wide call): its n_sel sorted entries (get(j)), its
+// uncapped count and its output row; solve the parked queries once `ring` wait.
+template <typename T, typename GetEntry>
+__device__ __forceinline__ void sel_push(const SelSpec<T>& sp, SelRing& rg, uint32_t found, uint32_t n_sel,
+                                         uint64_t row, GetEntry&& get) {
+    const int lane = threadIdx.x & 31;
+    const int stride = sp.ring + 1;
+    const uint32_t k = min(n_sel, sp.max_knn);
+    for (uint32_t j = lane; j < k; j += 32) rg.idx[(size_t)j * stride + rg.n] = get(j).idx;
+    if (lane == 0) {
+        rg.found[rg.n] = found;
+        rg.row[rg.n] = (uint32_t)row;
+    }
+    ++rg.n;
+    if (rg.n == sp.ring) sel_flush<T>(sp, rg);
+}
+
+// ------------------------------------------------------------------ general
+template <typename T, bool SEL>
 __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_constant__ SearchArgs<T> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -416,6 +555,13 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
                         : a.gbuf + ((size_t)blockIdx.x * kSearchWarps + wib) * a.cap;
     const uint64_t nwarps = (uint64_t)gridDim.x * kSearchWarps;
     const uint64_t m = a.qlist ? (uint64_t)*a.qcount : a.m;
+    SelRing rg{};
+    if constexpr (SEL) {
+        const size_t rb = sel_ring_bytes(a.sel.max_knn, a.sel.ring);
+        rg = sel_ring_at(smem_raw + kSearchWarps * sizeof(WarpSmem<T>) +
+                             (a.buf_in_smem ? (size_t)kSearchWarps * a.cap * sizeof(Entry<T>) : 0) + wib * rb,
+                         a.sel.max_knn, a.sel.ring);
+    }
 
     for (uint64_t qi = (uint64_t)blockIdx.x * kSearchWarps + wib; qi < m; qi += nwarps) {
         const uint64_t qpos = a.qlist ? a.qlist[qi] : qi;
@@ -534,10 +680,16 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
         int P = 1;
         while (P < (int)n_sel) P <<= 1;
         if (n_sel > 1) bitonic_sort<T>(buf, (int)n_sel, P);
-        emit_row<T>(a.mode, k, n_sel, found, a.rows_sorted ? qpos : row_base + qp.idx, a.out_idx, a.out_d2,
-                    a.out_found, a.fill_last, a.r2, [&](uint32_t j) { return buf[j]; });
+        if constexpr (SEL) {
+            sel_push<T>(a.sel, rg, found, n_sel, a.rows_sorted ? qpos : row_base + qp.idx,
+                        [&](uint32_t j) { return buf[j]; });
+        } else {
+            emit_row<T>(a.mode, k, n_sel, found, a.rows_sorted ? qpos : row_base + qp.idx, a.out_idx, a.out_d2,
+                        a.out_found, a.fill_last, a.r2, [&](uint32_t j) { return buf[j]; });
+        }
         __syncwarp();
     }
+    if constexpr (SEL) sel_flush<T>(a.sel, rg);
 }
 
 // ------------------------------------------------------------------ fast (float)
@@ -560,6 +712,7 @@ struct FastArgs {
     float r2;
     uint32_t cap;         // power of two, candidate keys per warp
     uint32_t cap_sorted;  // power of two, selected keys per warp
+    uint32_t chunk;       // consecutive queries per work item (first pass)
     const uint32_t* qlist;   // LIST pass: positions in `queries` to process ...
     const uint32_t* qcount;  // ... and their number (device)
     uint32_t* work;
@@ -571,12 +724,14 @@ struct FastArgs {
     int fill_last;
     int rows_sorted;  // output row = position in `queries`
     uint32_t* err;
+    SelSpec<float> sel;  // SEL instantiations
 };
 
 struct FastWarpSmem {
     uint32_t hist[kSelBins];
     uint32_t cursor[kSelBins];
     uint32_t run_start[32], run_len[32];
+    float kth_d2;  // squared distance of the k-th neighbour of the query just solved
 };
 
 __device__ __forceinline__ uint64_t make_key(float d2, uint32_t idx) {
@@ -606,26 +761,24 @@ __device__ __forceinline__ void bitonic_keys(uint64_t* keys, int n, int P) {
     }
 }
 
-// Sort the n_sel smallest of keys[0..count) into out (every key has d^2 <=
-// tau2): out is fully ordered up to the last bin that contains the n_sel-th
-// key. Returns false, writing nothing, when those bins hold more than out_cap
-// keys.
-__device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* keys, uint32_t count,
-                                              uint32_t n_sel, float tau2, uint64_t* out, uint32_t out_cap,
-                                              bool hist_ready = false) {
+// Hands the n_sel smallest of keys[0..count) (every key has d^2 <= tau2) to
+// emit(pos, key) with their final sorted positions pos < n_sel, in no
+// particular lane order. The selection histogram (ws->hist) is already
+// filled. Keys of the bins up to the one holding the n_sel-th key are
+// scattered into `out` by bin; a key's position is then its bin's start plus
+// the number of smaller keys in its bin (bins hold a handful of keys; keys are
+// unique since indices are). When exact ties crowd a bin the prefix is
+// bitonic-sorted instead. Returns false, emitting nothing, when those bins
+// hold more than out_cap keys.
+template <typename Emit>
+__device__ __forceinline__ bool select_emit(FastWarpSmem* ws, const uint64_t* keys, uint32_t count, uint32_t n_sel,
+                                            float tau2, uint64_t* out, uint32_t out_cap, Emit&& emit) {
     const int lane = threadIdx.x & 31;
     const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
-    if (!hist_ready) {
-        ws->hist[lane] = 0;
-        ws->hist[lane + 32] = 0;
-        __syncwarp();
-        for (uint32_t i = lane; i < count; i += 32) {
-            const float x = key_d2(keys[i]) * sb;
-            const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
-            atomicAdd(&ws->hist[bin], 1u);
-        }
-        __syncwarp();
-    }
+    const auto bin_of = [&](uint64_t key) {
+        const float x = key_d2(key) * sb;
+        return x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
+    };
     // lane owns bins 2*lane, 2*lane+1
     const uint32_t h0 = ws->hist[2 * lane], h1 = ws->hist[2 * lane + 1];
     uint32_t incl = h0 + h1;
@@ -658,8 +811,7 @@ __device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* 
     if (n_take > out_cap) return false;
     for (uint32_t i = lane; i < count; i += 32) {
         const uint64_t key = keys[i];
-        const float x = key_d2(key) * sb;
-        const int bin = x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x;
+        const int bin = bin_of(key);
         if (bin <= bstar) out[atomicAdd(&ws->cursor[bin], 1u)] = key;
     }
     __syncwarp();
@@ -669,26 +821,18 @@ __device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* 
         while (P < (int)n_take) P <<= 1;
         if (P > (int)out_cap) return false;
         bitonic_keys(out, (int)n_take, P);
+        for (uint32_t p = lane; p < n_sel; p += 32) emit(p, out[p]);
         __syncwarp();
         return true;
     }
-    // insertion sort inside each bin (a handful of keys each)
-#pragma unroll
-    for (int t = 0; t < 2; ++t) {
-        const int bin = 2 * lane + t;
-        if (bin <= bstar) {
-            const uint32_t end = ws->cursor[bin];
-            const uint32_t beg = end - (t ? h1 : h0);
-            for (uint32_t i = beg + 1; i < end; ++i) {
-                const uint64_t v = out[i];
-                uint32_t j = i;
-                while (j > beg && out[j - 1] > v) {
-                    out[j] = out[j - 1];
-                    --j;
-                }
-                out[j] = v;
-            }
-        }
+    // rank inside the bin; ws->cursor[bin] is now the bin's end
+    for (uint32_t p = lane; p < n_take; p += 32) {
+        const uint64_t key = out[p];
+        const int bin = bin_of(key);
+        const uint32_t end = ws->cursor[bin], beg = end - ws->hist[bin];
+        uint32_t pos = beg;
+        for (uint32_t q = beg; q < end; ++q) pos += out[q] < key;
+        if (pos < n_sel) emit(pos, key);
     }
     __syncwarp();
     return true;
@@ -697,7 +841,7 @@ __device__ __forceinline__ bool select_sorted(FastWarpSmem* ws, const uint64_t* 
 // LIST: a second pass over the queries whose key buffer overflowed in the
 // first (a.qlist / a.qcount), each with its pilot bound -- the first pass's
 // bound came from a solved neighbour and was too loose -- and a larger buffer.
-template <bool MULTI, bool LIST>
+template <bool MULTI, bool LIST, bool SEL>
 __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -705,9 +849,16 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
     uint64_t* keys = reinterpret_cast<uint64_t*>(smem_raw + kFastWarps * sizeof(FastWarpSmem)) +
                      (size_t)wib * (a.cap + a.cap_sorted);
     uint64_t* sorted = keys + a.cap;
+    SelRing rg{};
+    if constexpr (SEL) {
+        rg = sel_ring_at(smem_raw + kFastWarps * sizeof(FastWarpSmem) +
+                             (size_t)kFastWarps * (a.cap + a.cap_sorted) * sizeof(uint64_t) +
+                             wib * sel_ring_bytes(a.sel.max_knn, a.sel.ring),
+                         a.sel.max_knn, a.sel.ring);
+    }
     const uint32_t k = a.k;
     const uint64_t m = LIST ? (uint64_t)*a.qcount : a.m;
-    constexpr int chunk_len = LIST ? 1 : kChunk;  // list queries are few and costly: one per work item
+    const uint32_t chunk_len = LIST ? 1u : a.chunk;  // list queries are few and costly: one per work item
     for (;;) {
         uint32_t chunk = 0;
         if (lane == 0) chunk = atomicAdd(a.work, 1u);
@@ -732,88 +883,137 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
             }
             const GridParams& g = gv.g;
             const float q[3] = {qp.x, qp.y, qp.z};
-            float tau2;
-            bool strict;
-            if (a.mode == MODE_KNN) {
-                strict = false;
-                // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
-                // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
-                // neighbours within 0.9 d_k(p)): when it holds >= k points the k
-                // nearest are all among them, otherwise (count < k) the query goes
-                // to the list pass, which re-solves it with a pilot bound.
-                float bound = INFINITY;
-                if (!LIST && rdk >= 0.0f && rci == ci) {
-                    const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
-                    const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
-                }
-                bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
-                if (bound < INFINITY) {
-                    const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
-                    tau2 = t * t;
+            // kNN: a query whose optimistic bound fails is solved again right
+            // away with a pilot bound (no second launch and no tail for it)
+            bool retry = false;
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                float tau2;
+                bool strict;
+                bool used_pilot = false;
+                if (a.mode == MODE_KNN) {
+                    strict = false;
+                    // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
+                    // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
+                    // neighbours within 0.9 d_k(p)): when it holds >= k points the k
+                    // nearest are all among them, otherwise (count < k, or more
+                    // candidates than the buffer holds) the query is solved again at
+                    // once with a pilot bound.
+                    float bound = INFINITY;
+                    if (!LIST && !retry && rdk >= 0.0f && rci == ci) {
+                        const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
+                        const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
+                        if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
+                    }
+                    bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
+                    if (bound < INFINITY) {
+                        const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
+                        tau2 = t * t;
+                    } else {
+                        tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                        used_pilot = true;
+                    }
                 } else {
-                    tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                    strict = true;
+                    tau2 = a.r2;
                 }
-            } else {
-                strict = true;
-                tau2 = a.r2;
-            }
-            const float tf = sqrtf(tau2) * 1.000001f + g.margin;
-            const Box rb = region_box(g, q[0], q[1], q[2], tf);
-            uint32_t count = 0;
-            // the selection histogram is filled while collecting
-            const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
-            ws->hist[lane] = 0;
-            ws->hist[lane + 32] = 0;
-            __syncwarp();
-            visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
-                             [&](bool valid, float d2, uint32_t idx) {
-                                 const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
-                                 const uint32_t mask = __ballot_sync(FULL, take);
-                                 if (take) {
-                                     const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
-                                     if (pos < a.cap) keys[pos] = make_key(d2, idx);
-                                     const float x = d2 * sb;
-                                     atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
-                                 }
-                                 count += __popc(mask);
-                             });
-            __syncwarp();
-            const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
-            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
-            const bool ok = count <= a.cap && !short_knn &&
-                            (n_sel == 0 || select_sorted(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, true));
-            if (!ok) {
-                if (lane == 0) {
-                    const uint32_t slot = atomicAdd(a.ovf_count, 1u);
-                    a.ovf_list[slot] = (uint32_t)qi;
+                const float tf = sqrtf(tau2) * 1.000001f + g.margin;
+                const Box rb = region_box(g, q[0], q[1], q[2], tf);
+                uint32_t count = 0;
+                // the selection histogram is filled while collecting
+                const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
+                ws->hist[lane] = 0;
+                ws->hist[lane + 32] = 0;
+                __syncwarp();
+                visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
+                                 [&](bool valid, float d2, uint32_t idx) {
+                                     const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
+                                     const uint32_t mask = __ballot_sync(FULL, take);
+                                     if (take) {
+                                         const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
+                                         if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                                         const float x = d2 * sb;
+                                         atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
+                                     }
+                                     count += __popc(mask);
+                                 });
+                __syncwarp();
+                const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
+                const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
+                const uint64_t row = a.rows_sorted ? qi : row_base + qp.idx;
+                bool ok = count <= a.cap && !short_knn;
+                if (ok && n_sel > 0) {
+                    // each selected key goes straight to its place in the result row
+                    if constexpr (SEL) {
+                        const size_t stride = (size_t)a.sel.ring + 1;
+                        const uint32_t kcap = a.sel.max_knn;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            if (pos < kcap) rg.idx[pos * stride + rg.n] = (uint32_t)key;
+                        });
+                    } else if (a.mode == MODE_KNN) {
+                        uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + row * k;
+                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            oi[pos] = (uint32_t)key;
+                            if (od) od[pos] = key_d2(key);
+                            if (pos == k - 1) ws->kth_d2 = key_d2(key);
+                        });
+                    } else {
+                        int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
+                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            oi[pos] = (int32_t)(uint32_t)key;
+                            if (od) od[pos] = key_d2(key);
+                        });
+                    }
                 }
-                continue;
+                if (!ok) {
+                    if (a.mode == MODE_KNN && !LIST && !used_pilot) {
+                        retry = true;
+                        continue;
+                    }
+                    // still too many candidates (or a radius search's): the list pass
+                    if (lane == 0) {
+                        const uint32_t slot = atomicAdd(a.ovf_count, 1u);
+                        a.ovf_list[slot] = (uint32_t)qi;
+                    }
+                    break;
+                }
+                if constexpr (SEL) {
+                    // park the query; its lane solves it with the others of the ring
+                    if (lane == 0) {
+                        rg.found[rg.n] = count;
+                        rg.row[rg.n] = (uint32_t)row;
+                    }
+                    ++rg.n;
+                    if (rg.n == a.sel.ring) sel_flush<float>(a.sel, rg);
+                } else if (a.mode != MODE_KNN) {
+                    // nanoflann's radius row: -1 / 0 after the hits, radius^2 in the last slot of a short row
+                    int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
+                    float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                    for (uint32_t j = n_sel + lane; j < k; j += 32) {
+                        oi[j] = -1;
+                        if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : 0.0f;
+                    }
+                    if (a.out_found && lane == 0) a.out_found[row] = count;
+                }
+                if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
+                    rdk = sqrtf(ws->kth_d2);
+                    rx = q[0];
+                    ry = q[1];
+                    rz = q[2];
+                    rci = ci;
+                }
+                __syncwarp();
+                break;
             }
-            emit_row<float>(a.mode, k, n_sel, count, a.rows_sorted ? qi : row_base + qp.idx, a.out_idx, a.out_d2,
-                            a.out_found, a.fill_last, a.r2,
-                            [&](uint32_t j) {
-                                const uint64_t key = sorted[j];
-                                Entry<float> e;
-                                e.d2 = key_d2(key);
-                                e.idx = (uint32_t)key;
-                                return e;
-                            });
-            if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
-                rdk = sqrtf(key_d2(sorted[k - 1]));
-                rx = q[0];
-                ry = q[1];
-                rz = q[2];
-                rci = ci;
-            }
-            __syncwarp();
         }
     }
+    if constexpr (SEL) sel_flush<float>(a.sel, rg);
 }
 
-template <bool MULTI, bool LIST>
+template <bool MULTI, bool LIST, bool SEL = false>
 __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __grid_constant__ FastArgs a) {
-    fast_search_body<MULTI, LIST>(a);
+    fast_search_body<MULTI, LIST, SEL>(a);
 }
 
 // The single-cloud kNN pass, compiled for 10 resident blocks per SM (48
@@ -821,88 +1021,7 @@ __global__ void __launch_bounds__(kFastWarps * 32) fast_search_kernel(const __gr
 // natural 56 registers); the radius pass keeps its natural allocation (the
 // bound makes it 3-4% slower).
 __global__ void __launch_bounds__(kFastWarps * 32, 10) fast_knn_kernel(const __grid_constant__ FastArgs a) {
-    fast_search_body<false, false>(a);
-}
-
-// ------------------------------------------------------------------ selected
-constexpr int kSelThreads = 128;
-constexpr int kSelIdsPerLaunch = 32;
-
-template <typename T>
-struct SelArgs {
-    const T* xyz;
-    uint64_t n;
-    const int32_t* nbr;
-    const uint32_t* found;
-    uint32_t max_knn;
-    int n_ids, id_offset, out_ids;
-    int ids[kSelIdsPerLaunch];
-    int order;
-    T* out;
-};
-
-template <typename T>
-__device__ __forceinline__ void solve(const Cov<T>& c, int order, Pca<T>& p);
-template <>
-__device__ __forceinline__ void solve<float>(const Cov<float>& c, int order, Pca<float>& p) {
-    bool res;
-    pca_solve_f32(c, order, p, res);
-}
-template <>
-__device__ __forceinline__ void solve<double>(const Cov<double>& c, int order, Pca<double>& p) {
-    pca_solve_f64<double>(c, order, &p);
-}
-
-// include/pgeof.hpp:354-369: fewer than 2 points in the radius -> zeros;
-// otherwise PCA of the nearest min(found, max_knn) in (distance, index) order.
-template <typename T>
-__global__ void __launch_bounds__(kSelThreads) selected_pca_kernel(const __grid_constant__ SelArgs<T> a) {
-    using O = XOps<T>;
-    const uint64_t i = blockIdx.x * (uint64_t)kSelThreads + threadIdx.x;
-    if (i >= a.n) return;
-    T* row = a.out + i * a.out_ids + a.id_offset;
-    const uint32_t found = a.found[i];
-    if (found < 2) {
-        for (int t = 0; t < a.n_ids; ++t) row[t] = T(0);
-        return;
-    }
-    const uint32_t k = min(found, a.max_knn);
-    const int32_t* nb = a.nbr + i * a.max_knn;
-    T sx = 0, sy = 0, sz = 0;
-    for (uint32_t j = 0; j < k; ++j) {
-        const uint64_t id = (uint32_t)nb[j];
-        sx = O::add(sx, a.xyz[3 * id]);
-        sy = O::add(sy, a.xyz[3 * id + 1]);
-        sz = O::add(sz, a.xyz[3 * id + 2]);
-    }
-    const T kk = (T)k;
-    const T mx = O::div(sx, kk), my = O::div(sy, kk), mz = O::div(sz, kk);
-    T xx = 0, xy = 0, xz = 0, yy = 0, yz = 0, zz = 0;
-    for (uint32_t j = 0; j < k; ++j) {
-        const uint64_t id = (uint32_t)nb[j];
-        const T dx = O::sub(a.xyz[3 * id], mx), dy = O::sub(a.xyz[3 * id + 1], my),
-                dz = O::sub(a.xyz[3 * id + 2], mz);
-        xx = O::add(xx, O::mul(dx, dx));
-        xy = O::add(xy, O::mul(dx, dy));
-        xz = O::add(xz, O::mul(dx, dz));
-        yy = O::add(yy, O::mul(dy, dy));
-        yz = O::add(yz, O::mul(dy, dz));
-        zz = O::add(zz, O::mul(dz, dz));
-    }
-    Cov<T> c;
-    c.xx = O::div(xx, kk);
-    c.xy = O::div(xy, kk);
-    c.xz = O::div(xz, kk);
-    c.yy = O::div(yy, kk);
-    c.yz = O::div(yz, kk);
-    c.zz = O::div(zz, kk);
-    Pca<T> p;
-    solve<T>(c, a.order, p);
-    for (int t = 0; t < a.n_ids; ++t) {
-        T v = T(0);
-        if (!selected_feature<T>(p, a.ids[t], v)) v = T(0);
-        row[t] = v;
-    }
+    fast_search_body<false, false, false>(a);
 }
 
 template <typename T>
@@ -920,9 +1039,11 @@ int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoin
     const uint64_t want = mode == MODE_KNN ? std::max<uint64_t>(2ull * k, 128) : std::max<uint64_t>(4ull * k, 256);
     uint32_t cap = 1;
     while (cap < want) cap <<= 1;
-    const bool in_smem = general_smem_bytes<T>(cap, true) <= std::min(di->max_smem_optin, 200 * 1024);
-    const int smem = general_smem_bytes<T>(cap, in_smem);
-    auto kern = search_kernel<T>;
+    const int ring_smem = out.sel ? (int)(kSearchWarps * sel_ring_bytes(out.sel->max_knn, out.sel->ring)) : 0;
+    const bool in_smem =
+        general_smem_bytes<T>(cap, true) + ring_smem <= std::min(di->max_smem_optin, 200 * 1024);
+    const int smem = general_smem_bytes<T>(cap, in_smem) + ring_smem;
+    auto kern = out.sel ? search_kernel<T, true> : search_kernel<T, false>;
     int per_sm = 0;
     PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kSearchWarps * 32, smem, &per_sm));
     const uint64_t blocks = std::min<uint64_t>(ceil_div_u(m, kSearchWarps), (uint64_t)di->sm_count * per_sm);
@@ -949,7 +1070,10 @@ int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoin
     a.fill_last = out.radius_fill_last ? 1 : 0;
     a.rows_sorted = out.rows_in_query_order ? 1 : 0;
     a.err = device_error_word();
-    KernelTimer kt(qlist ? "overflow_search_kernel" : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel"),
+    if (out.sel) a.sel = *out.sel;
+    KernelTimer kt(qlist ? "overflow_search_kernel"
+                         : (out.sel ? "selected_search_kernel"
+                                    : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel")),
                    s);
     kern<<<(unsigned)blocks, kSearchWarps * 32, smem, s>>>(a);
     count_launch();
@@ -974,7 +1098,7 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
 // second fast pass (pilot bounds, a 1024-key buffer) before the general kernel.
 int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<float>* queries, uint64_t m, int mode,
                 uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, uint32_t* words2,
-                cudaStream_t s) {
+                cudaStream_t s, uint32_t chunk = kChunk) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     // candidate buffer: 256 keys for kNN, 512 for radius (or 4k); selected
@@ -985,12 +1109,16 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     uint32_t cap_sorted = 1;
     while (cap_sorted < k + k / 2 + 16) cap_sorted <<= 1;
     cap_sorted = std::min(cap_sorted, cap);
-    const int smem = (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap + cap_sorted) * sizeof(uint64_t)));
-    auto kern = ct.n ? fast_search_kernel<true, false>
-                     : (mode == MODE_KNN ? fast_knn_kernel : fast_search_kernel<false, false>);
+    const int ring_smem = out.sel ? (int)(kFastWarps * sel_ring_bytes(out.sel->max_knn, out.sel->ring)) : 0;
+    const int smem =
+        (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap + cap_sorted) * sizeof(uint64_t))) + ring_smem;
+    auto kern = out.sel ? fast_search_kernel<false, false, true>
+                        : (ct.n ? fast_search_kernel<true, false>
+                                : (mode == MODE_KNN ? fast_knn_kernel : fast_search_kernel<false, false>));
     int per_sm = 0;
     PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kFastWarps * 32, smem, &per_sm));
-    const uint64_t chunks = ceil_div_u(m, kChunk);
+    chunk = std::max<uint32_t>(chunk, 1u);
+    const uint64_t chunks = ceil_div_u(m, chunk);
     const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
     PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
     FastArgs a{};
@@ -1003,6 +1131,7 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     a.r2 = radius * radius;  // sq_search_radius in real_t, nn_search.hpp:98
     a.cap = cap;
     a.cap_sorted = cap_sorted;
+    a.chunk = chunk;
     a.work = words;
     a.ovf_count = words + 1;
     a.ovf_list = words + 8;
@@ -1012,8 +1141,10 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     a.fill_last = out.radius_fill_last ? 1 : 0;
     a.rows_sorted = out.rows_in_query_order ? 1 : 0;
     a.err = device_error_word();
+    if (out.sel) a.sel = *out.sel;
     {
-        KernelTimer kt(mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel", s);
+        KernelTimer kt(out.sel ? "selected_search_kernel" : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel"),
+                       s);
         kern<<<(unsigned)blocks, kFastWarps * 32, smem, s>>>(a);
     }
     count_launch();
@@ -1023,8 +1154,8 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
         uint32_t cap2 = 1;
         while (cap2 < std::max<uint64_t>(1024, 4ull * k)) cap2 <<= 1;
         const int smem2 =
-            (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t)));
-        auto kern2 = fast_search_kernel<false, true>;
+            (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t))) + ring_smem;
+        auto kern2 = out.sel ? fast_search_kernel<false, true, true> : fast_search_kernel<false, true>;
         int per_sm2 = 0;
         PGEOF_TRY(kernel_blocks_per_sm((const void*)kern2, kFastWarps * 32, smem2, &per_sm2));
         PGEOF_CUDA_TRY(cudaMemsetAsync(words2, 0, 8 * sizeof(uint32_t), s));
@@ -1072,7 +1203,7 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
 
 int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const SPoint<float>* pts, uint64_t n_points,
                         uint32_t k, uint32_t* indices, float* sqr_dist, uint32_t* work, uint32_t* ovf,
-                        cudaStream_t s) {
+                        cudaStream_t s, uint32_t chunk) {
     if (n_points == 0 || k == 0) return PGEOF_OK;
     GridView<float> gv{};
     gv.cell_start = cell_start;
@@ -1083,41 +1214,12 @@ int launch_search_batch(const CloudTable& ct, const uint32_t* cell_start, const 
     if (k > 128)
         return launch_general_view<float>(gv, ct, pts, n_points, nullptr, nullptr, MODE_KNN, k, 0.0f, out, s);
     (void)ovf;
-    return launch_fast(gv, ct, pts, n_points, MODE_KNN, k, 0.0f, out, work, nullptr, s);
-}
-
-template <typename T>
-int launch_selected_pca(const T* xyz, uint64_t n, const int32_t* nbr, const uint32_t* found, uint32_t max_knn,
-                        const int32_t* ids, int n_ids, T* out, cudaStream_t s) {
-    if (n == 0 || n_ids == 0) return PGEOF_OK;
-    SelArgs<T> a{};
-    a.xyz = xyz;
-    a.n = n;
-    a.nbr = nbr;
-    a.found = found;
-    a.max_knn = max_knn;
-    a.out_ids = n_ids;
-    a.order = eig_order();
-    a.out = out;
-    for (int off = 0; off < n_ids; off += kSelIdsPerLaunch) {
-        a.n_ids = std::min(kSelIdsPerLaunch, n_ids - off);
-        a.id_offset = off;
-        for (int t = 0; t < a.n_ids; ++t) a.ids[t] = ids[off + t];
-        KernelTimer kt("selected_pca_kernel", s);
-        selected_pca_kernel<T><<<ceil_div_u(n, kSelThreads), kSelThreads, 0, s>>>(a);
-        count_launch();
-        PGEOF_TRY(check_launch("selected_pca_kernel"));
-    }
-    return PGEOF_OK;
+    return launch_fast(gv, ct, pts, n_points, MODE_KNN, k, 0.0f, out, work, nullptr, s, chunk);
 }
 
 template int launch_search<float>(const GridIndex<float>&, const SPoint<float>*, const uint32_t*, uint64_t, int,
                                   uint32_t, float, const SearchOut<float>&, cudaStream_t);
 template int launch_search<double>(const GridIndex<double>&, const SPoint<double>*, const uint32_t*, uint64_t, int,
                                    uint32_t, double, const SearchOut<double>&, cudaStream_t);
-template int launch_selected_pca<float>(const float*, uint64_t, const int32_t*, const uint32_t*, uint32_t,
-                                        const int32_t*, int, float*, cudaStream_t);
-template int launch_selected_pca<double>(const double*, uint64_t, const int32_t*, const uint32_t*, uint32_t,
-                                         const int32_t*, int, double*, cudaStream_t);
 
 }  // namespace pgeof
