@@ -53,7 +53,7 @@ struct FeatArgs {
     uint32_t uniform_k;            // ptr == nullptr: row r is nn[r * uniform_k, (r + 1) * uniform_k)
     uint32_t row_base;             // this launch covers rows [row_base, row_base + n_points)
     int row_map_input;             // with row_map: row r also reads CSR row row_map[r].idx
-    uint32_t ks;                   // staged kernel: neighbours per row held in shared memory
+    uint32_t slab_words;           // SLAB kernel: index words per warp in shared memory
 };
 
 struct RowCloud {
@@ -95,53 +95,32 @@ __device__ __forceinline__ void gather_row(const uint32_t* nn_all, uint64_t b, u
 }
 
 
-// 16-byte global -> shared copy that holds no register while in flight
-// (cached in L2 only: a gathered point is not re-read by the same SM).
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(gmem_src) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// Copies the points of the CSR row at nn + b (count neighbours) into a column
-// of shared memory (entry j at col[j * stride]); indices are read four at a
-// time like gather_row, out-of-range ones flagged and replaced by point 0.
-__device__ __forceinline__ void stage_row(const uint32_t* nn_all, uint64_t b, uint32_t count, const float4* xyz4,
-                                          uint32_t n_xyz, uint32_t& flags, float4* col, int stride) {
-    const uint32_t* nn = nn_all + b;
-    auto clamp = [&](uint32_t id) {
-        if (id >= n_xyz) {
-            flags |= ERR_NN_RANGE;
-            id = 0;
-        }
-        return id;
-    };
+// gather_row over indices already in shared memory (idx[0 .. count)).
+template <typename F>
+__device__ __forceinline__ void gather_row_slab(const uint32_t* idx, uint32_t count, const float4* xyz4,
+                                                uint32_t n_xyz, uint32_t& flags, F&& f) {
     uint32_t j = 0;
-    while (j < count && (reinterpret_cast<uintptr_t>(nn + j) & 15u)) {
-        cp_async16(col + (size_t)j * stride, xyz4 + clamp(__ldg(nn + j)));
-        ++j;
-    }
     for (; j + 4 <= count; j += 4) {
-        const uint4 ids = __ldg(reinterpret_cast<const uint4*>(nn + j));
-        cp_async16(col + (size_t)j * stride, xyz4 + clamp(ids.x));
-        cp_async16(col + (size_t)(j + 1) * stride, xyz4 + clamp(ids.y));
-        cp_async16(col + (size_t)(j + 2) * stride, xyz4 + clamp(ids.z));
-        cp_async16(col + (size_t)(j + 3) * stride, xyz4 + clamp(ids.w));
+        const uint32_t i0 = idx[j], i1 = idx[j + 1], i2 = idx[j + 2], i3 = idx[j + 3];
+        const float4 p0 = gather_nb(xyz4, n_xyz, i0, flags), p1 = gather_nb(xyz4, n_xyz, i1, flags);
+        const float4 p2 = gather_nb(xyz4, n_xyz, i2, flags), p3 = gather_nb(xyz4, n_xyz, i3, flags);
+        f(j, p0);
+        f(j + 1, p1);
+        f(j + 2, p2);
+        f(j + 3, p3);
     }
-    for (; j < count; ++j) cp_async16(col + (size_t)j * stride, xyz4 + clamp(__ldg(nn + j)));
+    for (; j < count; ++j) f(j, gather_nb(xyz4, n_xyz, idx[j], flags));
 }
 
-// STAGE: the row's neighbours (up to a.ks of them) are copied once into this
-// thread's column of shared memory (cp.async, THREADS-strided, in front of the
-// output staging area) and both sweeps read them there -- one random gather
-// per neighbour instead of two. Longer rows gather twice from global memory.
-template <int S, bool MULTI, int THREADS = kFeatThreads, bool STAGE = false>
-__global__ void __launch_bounds__(THREADS) features_kernel(const __grid_constant__ FeatArgs a) {
+// SLAB: the CSR indices of a warp's 32 consecutive rows (one contiguous range
+// of nn when the rows are in CSR order) are read once into shared memory with
+// coalesced loads, and both sweeps take them from there -- instead of each
+// thread reading its own row's indices from global memory in both sweeps.
+// Rows outside the slab (too long, out of order) read global memory.
+template <int S, bool MULTI, bool SLAB = false>
+__global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
     extern __shared__ __align__(16) float smem_f[];
-    // STAGE: a.ks * THREADS float4 of points, then the output staging
-    float4* pts = reinterpret_cast<float4*>(smem_f);
-    float* stage = STAGE ? smem_f + (size_t)a.ks * THREADS * 4 : smem_f;  // THREADS * n_scales * 11
-    constexpr int kFeatThreads = THREADS;
+    float* stage = smem_f;  // kFeatThreads * n_scales * 11, then SLAB: a.slab_words per warp
     const int tid = threadIdx.x;
     const uint32_t i = a.row_base + blockIdx.x * kFeatThreads + tid;
     const int row_w = a.n_scales * 11;
@@ -149,8 +128,9 @@ __global__ void __launch_bounds__(THREADS) features_kernel(const __grid_constant
 
     uint32_t flags = 0;
     unsigned n_resolved = 0;
-    if (i < a.row_base + a.n_points) {
-        uint64_t b, e;
+    const bool row_ok = i < a.row_base + a.n_points;
+    uint64_t b = 0, e = 0;
+    if (row_ok) {
         const uint32_t ri = a.row_map_input ? a.row_map[i].idx : i;
         if (a.ptr) {
             b = __ldg(a.ptr + ri);
@@ -159,6 +139,24 @@ __global__ void __launch_bounds__(THREADS) features_kernel(const __grid_constant
             b = (uint64_t)i * a.uniform_k;
             e = b + a.uniform_k;
         }
+    }
+    const uint32_t* slab_idx = nullptr;  // this row's indices in shared memory
+    if constexpr (SLAB) {
+        const int lane = tid & 31;
+        const uint32_t vmask = __ballot_sync(0xffffffffu, row_ok);
+        if (vmask && !a.row_map_input) {
+            const int last = 31 - __clz(vmask);  // valid rows are a prefix of the warp
+            const uint64_t s0 = __shfl_sync(0xffffffffu, b, 0), s1 = __shfl_sync(0xffffffffu, e, last);
+            if (s1 >= s0 && s1 - s0 <= a.slab_words && s1 <= a.nnz) {
+                uint32_t* slab = reinterpret_cast<uint32_t*>(stage + (size_t)kFeatThreads * row_w) +
+                                 (size_t)(tid >> 5) * a.slab_words;
+                for (uint32_t w = lane; w < (uint32_t)(s1 - s0); w += 32) slab[w] = __ldg(a.nn + s0 + w);
+                __syncwarp();
+                if (row_ok && b >= s0 && e <= s1 && e >= b) slab_idx = slab + (b - s0);
+            }
+        }
+    }
+    if (row_ok) {
         uint32_t k_nn = 0;
         if (e < b || e > a.nnz) {
             flags |= ERR_PTR_RANGE;
@@ -194,18 +192,10 @@ __global__ void __launch_bounds__(THREADS) features_kernel(const __grid_constant
             }
         }
         if (n_active > 0) {
-            bool staged = false;
-            if constexpr (STAGE) {
-                if (kmax <= a.ks) {
-                    stage_row(a.nn, b, kmax, rc.xyz4, rc.n, flags, pts + tid, kFeatThreads);
-                    cp_async_wait_all();
-                    staged = true;
-                }
-            }
-            // neighbours [j0, j1) of the row in order, from shared memory or gathered
+            // neighbours [j0, j1) of the row in order, indices from the slab or global memory
             const auto sweep = [&](uint32_t j0, uint32_t j1, auto&& f) {
-                if (STAGE && staged) {
-                    for (uint32_t j = j0; j < j1; ++j) f(j, pts[(size_t)j * kFeatThreads + tid]);
+                if (SLAB && slab_idx) {
+                    gather_row_slab(slab_idx + j0, j1 - j0, rc.xyz4, rc.n, flags, f);
                 } else {
                     gather_row(a.nn, b + j0, j1 - j0, rc.xyz4, rc.n, flags, f);
                 }
@@ -633,40 +623,32 @@ int pad_xyz(const float* xyz, uint64_t n, float4* out, cudaStream_t s) {
     return check_launch("pad_xyz_kernel");
 }
 
-constexpr int kStageThreads = 64;
-
-// Deepest neighbour list the staged kernel holds in shared memory
-// (PGEOF_FEATURE_STAGE; default 0, i.e. never: on the 1M-point scene at
-// k = 50 the staged kernel took 0.57 ms against 0.48 ms for two gather sweeps,
-// its 64 KB per 64 rows leaving 6 warps per SM).
-uint32_t max_stage_depth() {
-    static const uint32_t v = [] {
-        const char* e = getenv("PGEOF_FEATURE_STAGE");
-        return e ? (uint32_t)strtoul(e, nullptr, 10) : 0u;
+// Index slabs (SLAB kernel) for single-scale passes; PGEOF_FEATURE_SLAB=0
+// turns them off.
+bool use_index_slab() {
+    static const bool v = [] {
+        const char* e = getenv("PGEOF_FEATURE_SLAB");
+        return e ? atoi(e) != 0 : true;
     }();
     return v;
 }
 
 template <int S>
 static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
-    if (a.ks > 0) {
-        constexpr int T = kStageThreads;
-        const size_t smem = (size_t)a.ks * T * sizeof(float4) + (size_t)T * a.n_scales * 11 * sizeof(float);
-        auto kern = a.n_clouds > 0 ? features_kernel<S, true, T, true> : features_kernel<S, false, T, true>;
-        int per_sm = 0;
-        PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, T, (int)smem, &per_sm));
-        if (per_sm > 0) {
-            KernelTimer kt("features_kernel", s);
-            kern<<<ceil_div_u(a.n_points, T), T, smem, s>>>(a);
-            count_launch();
-            return check_launch("features_kernel (staged)");
-        }
-    }
-    const size_t smem = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
+    const size_t stage_bytes = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
     const unsigned blocks = ceil_div_u(a.n_points, kFeatThreads);
     KernelTimer kt("features_kernel", s);
-    if (a.n_clouds > 0) features_kernel<S, true><<<blocks, kFeatThreads, smem, s>>>(a);
-    else features_kernel<S, false><<<blocks, kFeatThreads, smem, s>>>(a);
+    if (a.slab_words > 0) {
+        const size_t smem = stage_bytes + (size_t)(kFeatThreads / 32) * a.slab_words * sizeof(uint32_t);
+        auto kern = a.n_clouds > 0 ? features_kernel<S, true, true> : features_kernel<S, false, true>;
+        int per_sm = 0;
+        PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kFeatThreads, (int)smem, &per_sm));
+        kern<<<blocks, kFeatThreads, smem, s>>>(a);
+    } else if (a.n_clouds > 0) {
+        features_kernel<S, true><<<blocks, kFeatThreads, stage_bytes, s>>>(a);
+    } else {
+        features_kernel<S, false><<<blocks, kFeatThreads, stage_bytes, s>>>(a);
+    }
     count_launch();
     return check_launch("features_kernel");
 }
@@ -694,16 +676,19 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
     a.err = device_error_word();
     a.resolved = resolved;
     a.out = out;
-    const uint32_t depth = max_stage_depth();
     if (full) {
         a.full = 1;
         a.k_min = (uint32_t)std::min<uint64_t>(k_min, 0xffffffffull);
         a.n_scales = 1;
         a.out_scales = 1;
         a.scale_offset = 0;
-        // uniform rows: exactly their length; CSR rows: the depth limit
-        // (longer rows fall back to gathering twice)
-        a.ks = uniform_k ? (uniform_k <= depth ? uniform_k : 0) : depth;
+        // Index slab sized for uniform rows exactly, CSR rows up to 64 neighbours
+        // on average (longer warps read global memory). Single-scale passes
+        // only: on the 1M-point scene the slab takes the k = 50 compute_features
+        // pass from 0.485 to 0.454 ms, but the 3-scale pass (whose output
+        // staging already holds 33 floats per row) from 0.706 to 0.917 ms.
+        const uint32_t ks = uniform_k ? uniform_k : 64u;
+        a.slab_words = use_index_slab() && !a.row_map_input && ks <= 128 ? 32u * ks + 4u : 0u;
         return launch_features_s<1>(a, s);
     }
     a.full = 0;
@@ -713,8 +698,7 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
         a.n_scales = cnt;
         a.scale_offset = s0;
         for (int q = 0; q < cnt; ++q) a.scales[q] = scales[s0 + q];
-        const uint32_t kmax = *std::max_element(a.scales, a.scales + cnt);
-        a.ks = kmax <= depth ? kmax : 0;
+        a.slab_words = 0;
         int st;
         if (cnt == 1) st = launch_features_s<1>(a, s);
         else if (cnt == 2) st = launch_features_s<2>(a, s);

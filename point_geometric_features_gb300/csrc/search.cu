@@ -883,129 +883,117 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
             }
             const GridParams& g = gv.g;
             const float q[3] = {qp.x, qp.y, qp.z};
-            // kNN: a query whose optimistic bound fails is solved again right
-            // away with a pilot bound (no second launch and no tail for it)
-            bool retry = false;
-            for (int attempt = 0; attempt < 2; ++attempt) {
-                float tau2;
-                bool strict;
-                bool used_pilot = false;
-                if (a.mode == MODE_KNN) {
-                    strict = false;
-                    // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
-                    // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
-                    // neighbours within 0.9 d_k(p)): when it holds >= k points the k
-                    // nearest are all among them, otherwise (count < k, or more
-                    // candidates than the buffer holds) the query is solved again at
-                    // once with a pilot bound.
-                    float bound = INFINITY;
-                    if (!LIST && !retry && rdk >= 0.0f && rci == ci) {
-                        const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
-                        const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
-                        if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
-                    }
-                    bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
-                    if (bound < INFINITY) {
-                        const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
-                        tau2 = t * t;
-                    } else {
-                        tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
-                        used_pilot = true;
-                    }
+            float tau2;
+            bool strict;
+            if (a.mode == MODE_KNN) {
+                strict = false;
+                // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
+                // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
+                // neighbours within 0.9 d_k(p)): when it holds >= k points the k
+                // nearest are all among them, otherwise (count < k) the query goes
+                // to the list pass, which re-solves it with a pilot bound. (Solving
+                // such queries again at once in this pass measured slower: 1.35 ->
+                // 1.40 ms here for 0.23 -> 0.19 ms in the list passes.)
+                float bound = INFINITY;
+                if (!LIST && rdk >= 0.0f && rci == ci) {
+                    const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
+                    const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
+                    if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
+                }
+                bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
+                if (bound < INFINITY) {
+                    const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
+                    tau2 = t * t;
                 } else {
-                    strict = true;
-                    tau2 = a.r2;
+                    tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
                 }
-                const float tf = sqrtf(tau2) * 1.000001f + g.margin;
-                const Box rb = region_box(g, q[0], q[1], q[2], tf);
-                uint32_t count = 0;
-                // the selection histogram is filled while collecting
-                const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
-                ws->hist[lane] = 0;
-                ws->hist[lane + 32] = 0;
-                __syncwarp();
-                visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
-                                 [&](bool valid, float d2, uint32_t idx) {
-                                     const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
-                                     const uint32_t mask = __ballot_sync(FULL, take);
-                                     if (take) {
-                                         const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
-                                         if (pos < a.cap) keys[pos] = make_key(d2, idx);
-                                         const float x = d2 * sb;
-                                         atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
-                                     }
-                                     count += __popc(mask);
-                                 });
-                __syncwarp();
-                const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
-                const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
-                const uint64_t row = a.rows_sorted ? qi : row_base + qp.idx;
-                bool ok = count <= a.cap && !short_knn;
-                if (ok && n_sel > 0) {
-                    // each selected key goes straight to its place in the result row
-                    if constexpr (SEL) {
-                        const size_t stride = (size_t)a.sel.ring + 1;
-                        const uint32_t kcap = a.sel.max_knn;
-                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                            if (pos < kcap) rg.idx[pos * stride + rg.n] = (uint32_t)key;
-                        });
-                    } else if (a.mode == MODE_KNN) {
-                        uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + row * k;
-                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                            oi[pos] = (uint32_t)key;
-                            if (od) od[pos] = key_d2(key);
-                            if (pos == k - 1) ws->kth_d2 = key_d2(key);
-                        });
-                    } else {
-                        int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
-                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                            oi[pos] = (int32_t)(uint32_t)key;
-                            if (od) od[pos] = key_d2(key);
-                        });
-                    }
-                }
-                if (!ok) {
-                    if (a.mode == MODE_KNN && !LIST && !used_pilot) {
-                        retry = true;
-                        continue;
-                    }
-                    // still too many candidates (or a radius search's): the list pass
-                    if (lane == 0) {
-                        const uint32_t slot = atomicAdd(a.ovf_count, 1u);
-                        a.ovf_list[slot] = (uint32_t)qi;
-                    }
-                    break;
-                }
+            } else {
+                strict = true;
+                tau2 = a.r2;
+            }
+            const float tf = sqrtf(tau2) * 1.000001f + g.margin;
+            const Box rb = region_box(g, q[0], q[1], q[2], tf);
+            uint32_t count = 0;
+            // the selection histogram is filled while collecting
+            const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
+            ws->hist[lane] = 0;
+            ws->hist[lane + 32] = 0;
+            __syncwarp();
+            visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
+                             [&](bool valid, float d2, uint32_t idx) {
+                                 const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
+                                 const uint32_t mask = __ballot_sync(FULL, take);
+                                 if (take) {
+                                     const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
+                                     if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                                     const float x = d2 * sb;
+                                     atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
+                                 }
+                                 count += __popc(mask);
+                             });
+            __syncwarp();
+            const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
+            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
+            const uint64_t row = a.rows_sorted ? qi : row_base + qp.idx;
+            bool ok = count <= a.cap && !short_knn;
+            if (ok && n_sel > 0) {
+                // each selected key goes straight to its place in the result row
                 if constexpr (SEL) {
-                    // park the query; its lane solves it with the others of the ring
-                    if (lane == 0) {
-                        rg.found[rg.n] = count;
-                        rg.row[rg.n] = (uint32_t)row;
-                    }
-                    ++rg.n;
-                    if (rg.n == a.sel.ring) sel_flush<float>(a.sel, rg);
-                } else if (a.mode != MODE_KNN) {
-                    // nanoflann's radius row: -1 / 0 after the hits, radius^2 in the last slot of a short row
+                    const size_t stride = (size_t)a.sel.ring + 1;
+                    const uint32_t kcap = a.sel.max_knn;
+                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                        if (pos < kcap) rg.idx[pos * stride + rg.n] = (uint32_t)key;
+                    });
+                } else if (a.mode == MODE_KNN) {
+                    uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + row * k;
+                    float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                        oi[pos] = (uint32_t)key;
+                        if (od) od[pos] = key_d2(key);
+                        if (pos == k - 1) ws->kth_d2 = key_d2(key);
+                    });
+                } else {
                     int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
                     float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                    for (uint32_t j = n_sel + lane; j < k; j += 32) {
-                        oi[j] = -1;
-                        if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : 0.0f;
-                    }
-                    if (a.out_found && lane == 0) a.out_found[row] = count;
+                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                        oi[pos] = (int32_t)(uint32_t)key;
+                        if (od) od[pos] = key_d2(key);
+                    });
                 }
-                if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
-                    rdk = sqrtf(ws->kth_d2);
-                    rx = q[0];
-                    ry = q[1];
-                    rz = q[2];
-                    rci = ci;
-                }
-                __syncwarp();
-                break;
             }
+            if (!ok) {
+                if (lane == 0) {
+                    const uint32_t slot = atomicAdd(a.ovf_count, 1u);
+                    a.ovf_list[slot] = (uint32_t)qi;
+                }
+                continue;
+            }
+            if constexpr (SEL) {
+                // park the query; its lane solves it with the others of the ring
+                if (lane == 0) {
+                    rg.found[rg.n] = count;
+                    rg.row[rg.n] = (uint32_t)row;
+                }
+                ++rg.n;
+                if (rg.n == a.sel.ring) sel_flush<float>(a.sel, rg);
+            } else if (a.mode != MODE_KNN) {
+                // nanoflann's radius row: -1 / 0 after the hits, radius^2 in the last slot of a short row
+                int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
+                float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                for (uint32_t j = n_sel + lane; j < k; j += 32) {
+                    oi[j] = -1;
+                    if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : 0.0f;
+                }
+                if (a.out_found && lane == 0) a.out_found[row] = count;
+            }
+            if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
+                rdk = sqrtf(ws->kth_d2);
+                rx = q[0];
+                ry = q[1];
+                rz = q[2];
+                rci = ci;
+            }
+            __syncwarp();
         }
     }
     if constexpr (SEL) sel_flush<float>(a.sel, rg);
@@ -1071,7 +1059,7 @@ int launch_general_view(const GridView<T>& gv, const CloudTable& ct, const SPoin
     a.rows_sorted = out.rows_in_query_order ? 1 : 0;
     a.err = device_error_word();
     if (out.sel) a.sel = *out.sel;
-    KernelTimer kt(qlist ? "overflow_search_kernel"
+    KernelTimer kt(qlist ? "overflow_general_kernel"
                          : (out.sel ? "selected_search_kernel"
                                     : (mode == MODE_KNN ? "knn_search_kernel" : "radius_search_kernel")),
                    s);
@@ -1167,7 +1155,7 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
         a2.ovf_count = words2 + 1;
         a2.ovf_list = words2 + 8;
         {
-            KernelTimer kt("overflow_search_kernel", s);
+            KernelTimer kt("overflow_list_kernel", s);
             kern2<<<(unsigned)((uint64_t)di->sm_count * per_sm2), kFastWarps * 32, smem2, s>>>(a2);
         }
         count_launch();
