@@ -36,6 +36,7 @@
 // selected features (thread-level work, done by the whole warp at once). No
 // neighbour table reaches global memory.
 #include <algorithm>
+#include <cstdlib>
 
 #include "eig3.cuh"
 #include "kernels.cuh"
@@ -527,6 +528,31 @@ __device__ __forceinline__ void sel_flush(const SelSpec<T>& sp, SelRing& rg) {
     rg.n = 0;
 }
 
+// After the warps' loops (block-wide call): the queries still parked in the
+// block's rings are solved one per thread, so the block's leftovers take
+// ceil(total / 32) warps of solver instructions rather than every warp's
+// partly filled one -- small clouds leave a few queries in every ring, and
+// the solver's float64 instructions cost the same per warp whatever the
+// number of active lanes.
+template <typename T>
+__device__ __forceinline__ void sel_flush_block(const SelSpec<T>& sp, SelRing& rg, unsigned char* ring_base,
+                                                int n_warps) {
+    __shared__ int parked[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) parked[w] = rg.n;
+    __syncthreads();
+    int t = threadIdx.x, ww = 0;
+    while (ww < n_warps && t >= parked[ww]) {
+        t -= parked[ww];
+        ++ww;
+    }
+    if (ww < n_warps) {
+        const SelRing r = sel_ring_at(ring_base + ww * sel_ring_bytes(sp.max_knn, sp.ring), sp.max_knn, sp.ring);
+        sel_solve<T>(sp, r.idx + t, sp.ring + 1, r.found[t], r.row[t]);
+    }
+    rg.n = 0;
+}
+
 // Park one query (warp-wide call): its n_sel sorted entries (get(j)), its
 // uncapped count and its output row; solve the parked queries once `ring` wait.
 template <typename T, typename GetEntry>
@@ -556,11 +582,10 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
     const uint64_t nwarps = (uint64_t)gridDim.x * kSearchWarps;
     const uint64_t m = a.qlist ? (uint64_t)*a.qcount : a.m;
     SelRing rg{};
+    unsigned char* ring_base = smem_raw + kSearchWarps * sizeof(WarpSmem<T>) +
+                               (a.buf_in_smem ? (size_t)kSearchWarps * a.cap * sizeof(Entry<T>) : 0);
     if constexpr (SEL) {
-        const size_t rb = sel_ring_bytes(a.sel.max_knn, a.sel.ring);
-        rg = sel_ring_at(smem_raw + kSearchWarps * sizeof(WarpSmem<T>) +
-                             (a.buf_in_smem ? (size_t)kSearchWarps * a.cap * sizeof(Entry<T>) : 0) + wib * rb,
-                         a.sel.max_knn, a.sel.ring);
+        rg = sel_ring_at(ring_base + wib * sel_ring_bytes(a.sel.max_knn, a.sel.ring), a.sel.max_knn, a.sel.ring);
     }
 
     for (uint64_t qi = (uint64_t)blockIdx.x * kSearchWarps + wib; qi < m; qi += nwarps) {
@@ -689,7 +714,7 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
         }
         __syncwarp();
     }
-    if constexpr (SEL) sel_flush<T>(a.sel, rg);
+    if constexpr (SEL) sel_flush_block<T>(a.sel, rg, ring_base, kSearchWarps);
 }
 
 // ------------------------------------------------------------------ fast (float)
@@ -850,11 +875,10 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
                      (size_t)wib * (a.cap + a.cap_sorted);
     uint64_t* sorted = keys + a.cap;
     SelRing rg{};
+    unsigned char* ring_base =
+        smem_raw + kFastWarps * sizeof(FastWarpSmem) + (size_t)kFastWarps * (a.cap + a.cap_sorted) * sizeof(uint64_t);
     if constexpr (SEL) {
-        rg = sel_ring_at(smem_raw + kFastWarps * sizeof(FastWarpSmem) +
-                             (size_t)kFastWarps * (a.cap + a.cap_sorted) * sizeof(uint64_t) +
-                             wib * sel_ring_bytes(a.sel.max_knn, a.sel.ring),
-                         a.sel.max_knn, a.sel.ring);
+        rg = sel_ring_at(ring_base + wib * sel_ring_bytes(a.sel.max_knn, a.sel.ring), a.sel.max_knn, a.sel.ring);
     }
     const uint32_t k = a.k;
     const uint64_t m = LIST ? (uint64_t)*a.qcount : a.m;
@@ -996,7 +1020,7 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
             __syncwarp();
         }
     }
-    if constexpr (SEL) sel_flush<float>(a.sel, rg);
+    if constexpr (SEL) sel_flush_block<float>(a.sel, rg, ring_base, kFastWarps);
 }
 
 template <bool MULTI, bool LIST, bool SEL = false>
@@ -1091,8 +1115,13 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     PGEOF_TRY(current_device_info(&di));
     // candidate buffer: 256 keys for kNN, 512 for radius (or 4k); selected
     // prefix: k plus the few keys that share the k-th key's histogram bin
+    static const uint64_t knn_keys = [] {
+        const char* e = getenv("PGEOF_KNN_KEYS");  // tuning override of the kNN candidate buffer
+        const unsigned long v = e ? strtoul(e, nullptr, 10) : 256ul;
+        return (uint64_t)std::min<unsigned long>(std::max<unsigned long>(v, 64ul), 4096ul);
+    }();
     uint32_t cap = 1;
-    const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? 256 : 512, 4ull * k);
+    const uint64_t want = std::max<uint64_t>(mode == MODE_KNN ? knn_keys : 512, 4ull * k);
     while (cap < want) cap <<= 1;
     uint32_t cap_sorted = 1;
     while (cap_sorted < k + k / 2 + 16) cap_sorted <<= 1;
