@@ -907,117 +907,128 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
             }
             const GridParams& g = gv.g;
             const float q[3] = {qp.x, qp.y, qp.z};
-            float tau2;
-            bool strict;
-            if (a.mode == MODE_KNN) {
-                strict = false;
-                // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
-                // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
-                // neighbours within 0.9 d_k(p)): when it holds >= k points the k
-                // nearest are all among them, otherwise (count < k) the query goes
-                // to the list pass, which re-solves it with a pilot bound. (Solving
-                // such queries again at once in this pass measured slower: 1.35 ->
-                // 1.40 ms here for 0.23 -> 0.19 ms in the list passes.)
-                float bound = INFINITY;
-                if (!LIST && rdk >= 0.0f && rci == ci) {
-                    const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
-                    const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
-                }
-                bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
-                if (bound < INFINITY) {
-                    const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
-                    tau2 = t * t;
+            bool optimistic = false;  // the first try used a triangle bound
+            for (int attempt = 0; attempt < 2; ++attempt) {
+                float tau2;
+                bool strict;
+                if (a.mode == MODE_KNN) {
+                    strict = false;
+                    // From a solved neighbour p, d_k(q) <= d_k(p) + |q - p|. The radius
+                    // used is the optimistic d_k(p) + |q - p| / 2 (best over the lanes,
+                    // neighbours within 0.9 d_k(p)): when it holds >= k points the k
+                    // nearest are all among them; otherwise (count < k, ~2% of the
+                    // queries of the outdoor scene) the query is collected again at
+                    // once within the guaranteed d_k(p) + |q - p|. (A pilot bound for
+                    // that second try measured slower: its extra box pass costs more
+                    // than the list pass it saves.)
+                    float bound = INFINITY;
+                    if (!LIST && rdk >= 0.0f && rci == ci) {
+                        const float dx = q[0] - rx, dy = q[1] - ry, dz = q[2] - rz;
+                        const float dq = sqrtf(dx * dx + dy * dy + dz * dz);
+                        if (attempt == 0) {
+                            if (dq <= 0.9f * rdk) bound = rdk + 0.5f * dq;
+                        } else {
+                            bound = rdk + dq;
+                        }
+                    }
+                    bound = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(bound)));
+                    if (attempt == 0) optimistic = bound < INFINITY;
+                    if (bound < INFINITY) {
+                        const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
+                        tau2 = t * t;
+                    } else {
+                        tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                    }
                 } else {
-                    tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                    strict = true;
+                    tau2 = a.r2;
                 }
-            } else {
-                strict = true;
-                tau2 = a.r2;
-            }
-            const float tf = sqrtf(tau2) * 1.000001f + g.margin;
-            const Box rb = region_box(g, q[0], q[1], q[2], tf);
-            uint32_t count = 0;
-            // the selection histogram is filled while collecting
-            const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
-            ws->hist[lane] = 0;
-            ws->hist[lane + 32] = 0;
-            __syncwarp();
-            visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
-                             [&](bool valid, float d2, uint32_t idx) {
-                                 const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
-                                 const uint32_t mask = __ballot_sync(FULL, take);
-                                 if (take) {
-                                     const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
-                                     if (pos < a.cap) keys[pos] = make_key(d2, idx);
-                                     const float x = d2 * sb;
-                                     atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
-                                 }
-                                 count += __popc(mask);
-                             });
-            __syncwarp();
-            const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
-            const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
-            const uint64_t row = a.rows_sorted ? qi : row_base + qp.idx;
-            bool ok = count <= a.cap && !short_knn;
-            if (ok && n_sel > 0) {
-                // each selected key goes straight to its place in the result row
+                const float tf = sqrtf(tau2) * 1.000001f + g.margin;
+                const Box rb = region_box(g, q[0], q[1], q[2], tf);
+                uint32_t count = 0;
+                // the selection histogram is filled while collecting
+                const float sb = tau2 > 0.0f ? (float)kSelBins / tau2 : 0.0f;
+                ws->hist[lane] = 0;
+                ws->hist[lane + 32] = 0;
+                __syncwarp();
+                visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
+                                 [&](bool valid, float d2, uint32_t idx) {
+                                     const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
+                                     const uint32_t mask = __ballot_sync(FULL, take);
+                                     if (take) {
+                                         const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
+                                         if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                                         const float x = d2 * sb;
+                                         atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
+                                     }
+                                     count += __popc(mask);
+                                 });
+                __syncwarp();
+                const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
+                const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
+                const uint64_t row = a.rows_sorted ? qi : row_base + qp.idx;
+                bool ok = count <= a.cap && !short_knn;
+                if (ok && n_sel > 0) {
+                    // each selected key goes straight to its place in the result row
+                    if constexpr (SEL) {
+                        const size_t stride = (size_t)a.sel.ring + 1;
+                        const uint32_t kcap = a.sel.max_knn;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            if (pos < kcap) rg.idx[pos * stride + rg.n] = (uint32_t)key;
+                        });
+                    } else if (a.mode == MODE_KNN) {
+                        uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + row * k;
+                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            oi[pos] = (uint32_t)key;
+                            if (od) od[pos] = key_d2(key);
+                            if (pos == k - 1) ws->kth_d2 = key_d2(key);
+                        });
+                    } else {
+                        int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
+                        float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
+                        ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
+                            oi[pos] = (int32_t)(uint32_t)key;
+                            if (od) od[pos] = key_d2(key);
+                        });
+                    }
+                }
+                if (!ok) {
+                    if (attempt == 0 && optimistic && short_knn) continue;  // the guaranteed bound next
+                    if (lane == 0) {
+                        const uint32_t slot = atomicAdd(a.ovf_count, 1u);
+                        a.ovf_list[slot] = (uint32_t)qi;
+                    }
+                    break;
+                }
                 if constexpr (SEL) {
-                    const size_t stride = (size_t)a.sel.ring + 1;
-                    const uint32_t kcap = a.sel.max_knn;
-                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                        if (pos < kcap) rg.idx[pos * stride + rg.n] = (uint32_t)key;
-                    });
-                } else if (a.mode == MODE_KNN) {
-                    uint32_t* oi = static_cast<uint32_t*>(a.out_idx) + row * k;
-                    float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                        oi[pos] = (uint32_t)key;
-                        if (od) od[pos] = key_d2(key);
-                        if (pos == k - 1) ws->kth_d2 = key_d2(key);
-                    });
-                } else {
+                    // park the query; its lane solves it with the others of the ring
+                    if (lane == 0) {
+                        rg.found[rg.n] = count;
+                        rg.row[rg.n] = (uint32_t)row;
+                    }
+                    ++rg.n;
+                    if (rg.n == a.sel.ring) sel_flush<float>(a.sel, rg);
+                } else if (a.mode != MODE_KNN) {
+                    // nanoflann's radius row: -1 / 0 after the hits, radius^2 in the last slot of a short row
                     int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
                     float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                    ok = select_emit(ws, keys, count, n_sel, tau2, sorted, a.cap_sorted, [&](uint32_t pos, uint64_t key) {
-                        oi[pos] = (int32_t)(uint32_t)key;
-                        if (od) od[pos] = key_d2(key);
-                    });
+                    for (uint32_t j = n_sel + lane; j < k; j += 32) {
+                        oi[j] = -1;
+                        if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : 0.0f;
+                    }
+                    if (a.out_found && lane == 0) a.out_found[row] = count;
                 }
-            }
-            if (!ok) {
-                if (lane == 0) {
-                    const uint32_t slot = atomicAdd(a.ovf_count, 1u);
-                    a.ovf_list[slot] = (uint32_t)qi;
+                if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
+                    rdk = sqrtf(ws->kth_d2);
+                    rx = q[0];
+                    ry = q[1];
+                    rz = q[2];
+                    rci = ci;
                 }
-                continue;
+                __syncwarp();
+                break;
             }
-            if constexpr (SEL) {
-                // park the query; its lane solves it with the others of the ring
-                if (lane == 0) {
-                    rg.found[rg.n] = count;
-                    rg.row[rg.n] = (uint32_t)row;
-                }
-                ++rg.n;
-                if (rg.n == a.sel.ring) sel_flush<float>(a.sel, rg);
-            } else if (a.mode != MODE_KNN) {
-                // nanoflann's radius row: -1 / 0 after the hits, radius^2 in the last slot of a short row
-                int32_t* oi = static_cast<int32_t*>(a.out_idx) + row * k;
-                float* od = a.out_d2 ? a.out_d2 + row * k : nullptr;
-                for (uint32_t j = n_sel + lane; j < k; j += 32) {
-                    oi[j] = -1;
-                    if (od) od[j] = (a.fill_last && j == k - 1) ? a.r2 : 0.0f;
-                }
-                if (a.out_found && lane == 0) a.out_found[row] = count;
-            }
-            if (!LIST && a.mode == MODE_KNN && lane == (int)(qi & 31)) {
-                rdk = sqrtf(ws->kth_d2);
-                rx = q[0];
-                ry = q[1];
-                rz = q[2];
-                rci = ci;
-            }
-            __syncwarp();
         }
     }
     if constexpr (SEL) sel_flush_block<float>(a.sel, rg, ring_base, kFastWarps);
@@ -1104,10 +1115,10 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
 }
 
 // The fast kernel over `queries` (cell order), then the general kernel over the
-// queries whose buffer overflowed. `words`: 8 zeroed words + m words.
-// `words`: 8 + m words of scratch (work counter, overflow count, overflow
-// list). With `words2` (another 8 + m words) the overflowing queries get a
-// second fast pass (pilot bounds, a 1024-key buffer) before the general kernel.
+// queries whose buffer overflowed. `words`: 8 + m words of scratch (work
+// counter, overflow count, overflow list). With `words2` (another 2 (8 + m)
+// words) the overflowing queries get two list passes of the fast kernel
+// (pilot bounds, 1024- then 4096-key buffers) before the general kernel.
 int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<float>* queries, uint64_t m, int mode,
                 uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, uint32_t* words2,
                 cudaStream_t s, uint32_t chunk = kChunk) {
@@ -1167,29 +1178,43 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     count_launch();
     PGEOF_TRY(check_launch("fast_search_kernel"));
     if (words2 && !ct.n) {
-        // second pass over the overflow list, sized on the device
-        uint32_t cap2 = 1;
-        while (cap2 < std::max<uint64_t>(1024, 4ull * k)) cap2 <<= 1;
-        const int smem2 =
-            (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t))) + ring_smem;
-        auto kern2 = out.sel ? fast_search_kernel<false, true, true> : fast_search_kernel<false, true>;
-        int per_sm2 = 0;
-        PGEOF_TRY(kernel_blocks_per_sm((const void*)kern2, kFastWarps * 32, smem2, &per_sm2));
-        PGEOF_CUDA_TRY(cudaMemsetAsync(words2, 0, 8 * sizeof(uint32_t), s));
-        FastArgs a2 = a;
-        a2.cap = cap2;
-        a2.qlist = a.ovf_list;
-        a2.qcount = a.ovf_count;
-        a2.work = words2;
-        a2.ovf_count = words2 + 1;
-        a2.ovf_list = words2 + 8;
-        {
-            KernelTimer kt("overflow_list_kernel", s);
-            kern2<<<(unsigned)((uint64_t)di->sm_count * per_sm2), kFastWarps * 32, smem2, s>>>(a2);
+        // List passes over the overflowing queries (one query per work item,
+        // a pilot bound, a larger buffer), sized on the device: 1024 keys, then
+        // 4096 keys for the few that still overflow, and the general kernel
+        // (refinement passes) for whatever is left -- usually nothing. The
+        // small first list buffer keeps that pass's occupancy for its
+        // thousands of queries; the second pass spares the general kernel's
+        // refinement passes, whose latency made its launch long.
+        const uint32_t* in_list = a.ovf_list;
+        const uint32_t* in_count = a.ovf_count;
+        for (int pass = 0; pass < 2; ++pass) {
+            uint32_t* w = words2 + (size_t)pass * (m + 8);
+            uint32_t cap2 = 1;
+            while (cap2 < std::max<uint64_t>(pass == 0 ? 1024 : 4096, 4ull * k)) cap2 <<= 1;
+            const int smem2 =
+                (int)(kFastWarps * (sizeof(FastWarpSmem) + (size_t)(cap2 + cap_sorted) * sizeof(uint64_t))) +
+                ring_smem;
+            auto kern2 = out.sel ? fast_search_kernel<false, true, true> : fast_search_kernel<false, true>;
+            int per_sm2 = 0;
+            PGEOF_TRY(kernel_blocks_per_sm((const void*)kern2, kFastWarps * 32, smem2, &per_sm2));
+            PGEOF_CUDA_TRY(cudaMemsetAsync(w, 0, 8 * sizeof(uint32_t), s));
+            FastArgs a2 = a;
+            a2.cap = cap2;
+            a2.qlist = in_list;
+            a2.qcount = in_count;
+            a2.work = w;
+            a2.ovf_count = w + 1;
+            a2.ovf_list = w + 8;
+            {
+                KernelTimer kt("overflow_list_kernel", s);
+                kern2<<<(unsigned)((uint64_t)di->sm_count * per_sm2), kFastWarps * 32, smem2, s>>>(a2);
+            }
+            count_launch();
+            PGEOF_TRY(check_launch("fast_search_kernel(list)"));
+            in_list = a2.ovf_list;
+            in_count = a2.ovf_count;
         }
-        count_launch();
-        PGEOF_TRY(check_launch("fast_search_kernel(list)"));
-        return launch_general_view<float>(gv, ct, queries, m, a2.ovf_list, a2.ovf_count, mode, k, radius, out, s);
+        return launch_general_view<float>(gv, ct, queries, m, in_list, in_count, mode, k, radius, out, s);
     }
     // queries whose key buffer overflowed: the general kernel, sized on the device
     return launch_general_view<float>(gv, ct, queries, m, a.ovf_list, a.ovf_count, mode, k, radius, out, s);
@@ -1208,7 +1233,7 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
         if (k > 128 || m >= 0xffffffffull)
             return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
         Scratch ctl;
-        PGEOF_TRY(ctl.alloc(2 * (m + 8) * sizeof(uint32_t), s));
+        PGEOF_TRY(ctl.alloc(3 * (m + 8) * sizeof(uint32_t), s));
         GridView<float> gv;
         gv.g = grid.g;
         gv.cell_start = grid.cell_start;
