@@ -250,7 +250,8 @@ int pgeof_batch_plan_create(const float* xyz, const int64_t* offsets, int64_t n_
                             pgeof_batch_plan* out);
 int pgeof_batch_plan_launch(pgeof_batch_plan plan, pgeof_stream_t stream);
 /* The parameters a plan runs with: cell occupancy factor (times the default
- * knn / 3.5 points per cell), queries per search work item, the pipeline time
+ * knn / 3.5 points per cell), queries per search work item (0: guided items,
+ * long while many queries remain, short at the end), the pipeline time
  * with them and with the defaults (1.0, 16) at tuning, and whether they came
  * from the shape-class cache. Any output pointer may be NULL. */
 int pgeof_batch_plan_info(pgeof_batch_plan plan, float* cell_factor, uint32_t* queries_per_item, float* tuned_ms,

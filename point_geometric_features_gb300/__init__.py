@@ -438,7 +438,8 @@ class BatchPlan:
         creation, or reused from an earlier plan of the same shape class) and
         the pipeline times measured with them and with the defaults."""
         cell, chunk, tuned, dflt, cached = _ext._batch_plan_info(self._h)
-        return {"cell_factor": round(float(cell), 3), "queries_per_work_item": int(chunk),
+        return {"cell_factor": round(float(cell), 3),
+                "queries_per_work_item": int(chunk) if chunk else "guided (64 down to 4)",
                 "warps_per_query": 1, "tuned_ms": round(float(tuned), 4), "default_ms": round(float(dflt), 4),
                 "from_cache": bool(cached)}
 

@@ -304,7 +304,8 @@ int batch_scan(BatchWorkspace& w, cudaStream_t s);
 // Speed parameters of the pipeline (results never depend on them): the grid
 // cell occupancy target as a factor of the default k / 3.5 points per cell
 // (each cloud's edge is still fitted to its own density), and the consecutive
-// queries of one search work item.
+// queries of one search work item (0: guided items, long while many queries
+// remain and short at the end).
 struct BatchTune {
     float cell = 1.0f;
     uint32_t chunk = 16;
@@ -403,7 +404,7 @@ int log2_bucket(double v) { return v >= 1.0 ? (int)std::floor(std::log2(v)) : 0;
 // own data and keeps the fastest second run.
 int autotune(BatchPlan* plan, const float* xyz, uint32_t* indices, float* sqr_dist, float* features, cudaStream_t s) {
     static const float kCells[3] = {0.6f, 1.0f, 1.6f};
-    static const uint32_t kChunks[3] = {8, 16, 32};
+    static const uint32_t kChunks[4] = {0, 8, 16, 32};  // 0: guided items (64 shrinking to 4)
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     PGEOF_CUDA_TRY(cudaEventCreate(&e0));
     if (cudaEventCreate(&e1) != cudaSuccess) {

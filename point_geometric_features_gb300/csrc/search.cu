@@ -720,10 +720,15 @@ __global__ void __launch_bounds__(kSearchWarps * 32) search_kernel(const __grid_
 // ------------------------------------------------------------------ fast (float)
 constexpr int kFastWarps = 4;
 // Consecutive queries per work item. Small items keep the warps' finishing
-// times even: per-query cost varies several-fold across a scene (walls and
-// cylinders vs open ground), and with 64-query items the last items left warps
-// idle for a quarter of the kernel.
-constexpr int kChunk = 16;
+// times even (per-query cost varies several-fold across a scene: walls and
+// cylinders vs open ground), long items start fewer chunks, each of which needs
+// a pilot bound for its first query. A single search uses guided items of
+// remaining / (4 x warps) queries, between 4 and 64 (1M-point scene, k = 50:
+// fixed 8 / 16 / 32 / 64-query items 1.354 / 1.379 / 1.479 / 1.675 ms; guided
+// 1.30 ms -- long items early, short ones at the end).
+constexpr int kChunkMax = 64;
+constexpr int kChunkMin = 4;
+constexpr int kGuide = 4;
 constexpr int kSelBins = 64;     // selection histogram
 constexpr int kMaxInBin = 24;    // larger bins (exact ties) fall back to a bitonic sort
 
@@ -737,7 +742,9 @@ struct FastArgs {
     float r2;
     uint32_t cap;         // power of two, candidate keys per warp
     uint32_t cap_sorted;  // power of two, selected keys per warp
-    uint32_t chunk;       // consecutive queries per work item (first pass)
+    uint32_t chunk;       // consecutive queries per work item (first pass): the largest
+    uint32_t chunk_min;   // ... and the smallest: items shrink to remaining / guide_div
+    uint32_t guide_div;
     const uint32_t* qlist;   // LIST pass: positions in `queries` to process ...
     const uint32_t* qcount;  // ... and their number (device)
     uint32_t* work;
@@ -882,14 +889,30 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
     }
     const uint32_t k = a.k;
     const uint64_t m = LIST ? (uint64_t)*a.qcount : a.m;
-    const uint32_t chunk_len = LIST ? 1u : a.chunk;  // list queries are few and costly: one per work item
     for (;;) {
-        uint32_t chunk = 0;
-        if (lane == 0) chunk = atomicAdd(a.work, 1u);
-        chunk = __shfl_sync(FULL, chunk, 0);
-        const uint64_t q0 = (uint64_t)chunk * chunk_len;
+        // Guided work items: a.chunk consecutive queries while many remain
+        // (fewer chunk starts, hence fewer pilot bounds), shrinking to
+        // remaining / guide_div and at least a.chunk_min towards the end, so
+        // that warps finish together. List queries are few and costly: one
+        // per item.
+        uint32_t start = 0, len = 1;
+        if (lane == 0) {
+            if (!LIST) {
+                len = a.chunk;
+                if (a.chunk_min < a.chunk) {
+                    const uint32_t seen = __ldcg(a.work);
+                    const uint64_t rem = seen < m ? m - seen : 0;
+                    const uint64_t g = rem / a.guide_div;
+                    len = g >= a.chunk ? a.chunk : (g <= a.chunk_min ? a.chunk_min : (uint32_t)g);
+                }
+            }
+            start = atomicAdd(a.work, len);
+        }
+        start = __shfl_sync(FULL, start, 0);
+        len = __shfl_sync(FULL, len, 0);
+        const uint64_t q0 = start;
         if (q0 >= m) break;
-        const uint64_t q1 = min(q0 + (uint64_t)chunk_len, m);
+        const uint64_t q1 = min(q0 + (uint64_t)len, m);
         // the last 32 solved queries of this chunk, one per lane: position and d_k
         float rx = 0.0f, ry = 0.0f, rz = 0.0f, rdk = -1.0f;
         int rci = -1;
@@ -1121,7 +1144,7 @@ int launch_general(const GridIndex<T>& grid, const SPoint<T>* queries, uint64_t 
 // (pilot bounds, 1024- then 4096-key buffers) before the general kernel.
 int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<float>* queries, uint64_t m, int mode,
                 uint32_t k, float radius, const SearchOut<float>& out, uint32_t* words, uint32_t* words2,
-                cudaStream_t s, uint32_t chunk = kChunk) {
+                cudaStream_t s, uint32_t chunk = 0) {
     const DeviceInfo* di;
     PGEOF_TRY(current_device_info(&di));
     // candidate buffer: 256 keys for kNN, 512 for radius (or 4k); selected
@@ -1145,9 +1168,23 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
                                 : (mode == MODE_KNN ? fast_knn_kernel : fast_search_kernel<false, false>));
     int per_sm = 0;
     PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kFastWarps * 32, smem, &per_sm));
-    chunk = std::max<uint32_t>(chunk, 1u);
-    const uint64_t chunks = ceil_div_u(m, chunk);
-    const uint64_t blocks = std::min<uint64_t>(ceil_div_u(chunks, kFastWarps), (uint64_t)di->sm_count * per_sm);
+    // Queries per work item: a fixed count when the caller gives one (batch
+    // plans tune it), else guided items from kChunkMax down to kChunkMin
+    // (PGEOF_KNN_CHUNK / PGEOF_KNN_CHUNK_MIN override them for tuning).
+    static const uint32_t guided_max = [] {
+        const char* e = getenv("PGEOF_KNN_CHUNK");
+        const unsigned long v = e ? strtoul(e, nullptr, 10) : (unsigned long)kChunkMax;
+        return (uint32_t)std::min<unsigned long>(std::max<unsigned long>(v, 1ul), 1024ul);
+    }();
+    static const uint32_t guided_min = [] {
+        const char* e = getenv("PGEOF_KNN_CHUNK_MIN");
+        const unsigned long v = e ? strtoul(e, nullptr, 10) : (unsigned long)kChunkMin;
+        return (uint32_t)std::min<unsigned long>(std::max<unsigned long>(v, 1ul), 1024ul);
+    }();
+    const uint32_t chunk_max = chunk ? chunk : guided_max;
+    const uint32_t chunk_min = chunk ? chunk : std::min(guided_min, guided_max);
+    const uint64_t items = ceil_div_u(m, chunk_min);
+    const uint64_t blocks = std::min<uint64_t>(ceil_div_u(items, kFastWarps), (uint64_t)di->sm_count * per_sm);
     PGEOF_CUDA_TRY(cudaMemsetAsync(words, 0, 8 * sizeof(uint32_t), s));
     FastArgs a{};
     a.gv = gv;
@@ -1159,7 +1196,14 @@ int launch_fast(const GridView<float>& gv, const CloudTable& ct, const SPoint<fl
     a.r2 = radius * radius;  // sq_search_radius in real_t, nn_search.hpp:98
     a.cap = cap;
     a.cap_sorted = cap_sorted;
-    a.chunk = chunk;
+    a.chunk = chunk_max;
+    a.chunk_min = chunk_min;
+    static const uint64_t guide = [] {
+        const char* e = getenv("PGEOF_KNN_GUIDE");  // tuning override: items shrink to remaining / (guide x warps)
+        const unsigned long v = e ? strtoul(e, nullptr, 10) : (unsigned long)kGuide;
+        return (uint64_t)std::min<unsigned long>(std::max<unsigned long>(v, 1ul), 64ul);
+    }();
+    a.guide_div = (uint32_t)std::max<uint64_t>(1, guide * blocks * kFastWarps);
     a.work = words;
     a.ovf_count = words + 1;
     a.ovf_list = words + 8;
@@ -1230,7 +1274,7 @@ int launch_search(const GridIndex<T>& grid, const SPoint<T>* queries, const uint
     if constexpr (sizeof(T) != sizeof(float)) {
         return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
     } else {
-        if (k > 128 || m >= 0xffffffffull)
+        if (k > 128 || m >= 0xfff00000ull)  // 32-bit work counters with headroom for the last items
             return launch_general<T>(grid, queries, m, nullptr, nullptr, mode, k, radius, out, s);
         Scratch ctl;
         PGEOF_TRY(ctl.alloc(3 * (m + 8) * sizeof(uint32_t), s));
