@@ -738,6 +738,9 @@ def run_features(args):
     for _ in range(max(args.warmup, 3)):
         out = pgeof.compute_features(t, nn, ptr, check=False)
     torch.cuda.synchronize()
+    clocks = ClockSampler(smi_index())
+    clocks.start()
+    time.sleep(0.2)
     pgeof.profile_kernels(True)
     pgeof.kernel_profile()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -748,6 +751,7 @@ def run_features(args):
         out = pgeof.compute_features(t, nn, ptr, check=False)
         stops[i].record()
     torch.cuda.synchronize()
+    clk = clocks.stop()
     prof = pgeof.kernel_profile()
     pgeof.profile_kernels(False)
     pgeof.check_device_errors()
@@ -783,6 +787,7 @@ def run_features(args):
         "f64": {"ms_per_step": round(ms64, 4), "value": round(N_POINTS / ms64 * 1e3, 1), "unit": UNIT,
                 "max_scaled_diff_vs_f32": f64_dev,
                 "path": "compute_features on a float64 CUDA tensor (real_t = double instantiation)"},
+        "clocks": clk,
     }
 
 
@@ -816,6 +821,8 @@ def run_index(args):
         return outs
 
     res = {}
+    clocks = ClockSampler(smi_index())
+    clocks.start()
     for name, fn in (("index", step_index), ("per_call", step_call)):
         for _ in range(max(args.warmup, 3)):
             outs = fn()
@@ -827,6 +834,7 @@ def run_index(args):
         b.record()
         torch.cuda.synchronize()
         res[name] = (a.elapsed_time(b) / args.steps, outs)
+    clk = clocks.stop()
     for (ai, ad), (bi, bd) in zip(res["index"][1], res["per_call"][1]):
         assert torch.equal(ai.view(torch.int32), bi.view(torch.int32)) and torch.equal(ad, bd)
     ix.close()
@@ -835,7 +843,7 @@ def run_index(args):
         "metric": "points/s resident-index searches (kNN k=10,20,50 + radius 0.5/64), 1M pts", "workload": "index",
         "value": round(N_POINTS / ms_ix * 1e3, 1), "unit": UNIT, "ms_per_step": round(ms_ix, 4),
         "per_call_ms_per_step": round(ms_call, 4), "index_build_ms": round(build_ms, 3), "steps": args.steps,
-        "dtype": "f32", "results_equal": True,
+        "dtype": "f32", "results_equal": True, "clocks": clk,
         "config": {"workload": "1M-point outdoor scene, 3 kNN + 1 radius search per step on one resident grid",
                    "points": N_POINTS, "k_hint": K, "l2": "outputs (1 GB per step) larger than L2"},
     }
@@ -869,12 +877,15 @@ def run_refbench(args):
             ts.append((_t.perf_counter() - t0) * 1e3)
         return float(np.median(ts))
 
+    clocks = ClockSampler(smi_index())
+    clocks.start()
     out = {
         "knn_search_1M_k50_ms": med(lambda: pgeof.knn_search(xyz, xyz, 50), args.steps),
         "radius_search_1M_r0.2_max30_ms": med(lambda: pgeof.radius_search(xyz, xyz, 0.2, 30), args.steps),
         "selected_10k_f64_r5_max50_ms": med(
             lambda: pgeof.compute_features_selected(small, 5.0, 50, [pgeof.Verticality]), args.steps),
     }
+    clk = clocks.stop()
     if not args.no_cpu_baseline:
         def scipy_knn():
             cKDTree(xyz).query(xyz, k=50, workers=-1)
@@ -890,6 +901,7 @@ def run_refbench(args):
         "config": {"workload": "tests/bench_knn.py and tests/bench_jakteristics.py shapes, seeded",
                    "host_threads": os.cpu_count()},
         **{k: round(v, 3) for k, v in out.items()},
+        "clocks": clk,
     }
 
 
