@@ -33,11 +33,31 @@ struct Cov {
     T xx, xy, xz, yy, yz, zz;
 };
 
-// One Jacobi rotation annihilating a[P][Q] (P < Q). Mirrors the CPU oracle's
-// solver operation for operation (explicit rounding, no fused multiply-add).
-template <int P, int Q, typename T, bool VEC>
+// Division and square root of a rotation's parameters: IEEE-rounded (the
+// oracle's arithmetic, used by the exact solver) or the hardware reciprocal
+// and reciprocal square root (FAST, float only). Any rotation angle that keeps
+// c^2 + s^2 = 1 to working precision serves Jacobi; the float solver's
+// eigenvalues are refined afterwards as Rayleigh quotients.
+template <typename T, bool FAST>
+struct RotOps {
+    static __device__ __forceinline__ T div(T a, T b) { return XOps<T>::div(a, b); }
+    static __device__ __forceinline__ T inv_sqrt1p(T x) { return XOps<T>::div(T(1), XOps<T>::sqrt_(XOps<T>::add(T(1), x))); }
+    static __device__ __forceinline__ T sqrt1p(T x) { return XOps<T>::sqrt_(XOps<T>::add(T(1), x)); }
+};
+template <>
+struct RotOps<float, true> {
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float inv_sqrt1p(float x) { return rsqrtf(1.0f + x); }
+    static __device__ __forceinline__ float sqrt1p(float x) { return sqrtf(1.0f + x); }
+};
+
+// One Jacobi rotation annihilating a[P][Q] (P < Q). Without FAST it mirrors the
+// CPU oracle's solver operation for operation (explicit rounding, no fused
+// multiply-add).
+template <int P, int Q, typename T, bool VEC, bool FAST = false>
 __device__ __forceinline__ void jacobi_rotate(T (&a)[3][3], T (&v)[3][3], bool late) {
     using O = XOps<T>;
+    using RO = RotOps<T, FAST>;
     constexpr int R = 3 - P - Q;
     const T apq = a[P][Q];
     if (apq == T(0)) return;
@@ -49,15 +69,15 @@ __device__ __forceinline__ void jacobi_rotate(T (&a)[3][3], T (&v)[3][3], bool l
     const T h = O::sub(a[Q][Q], a[P][P]);
     T t;
     if (O::add(fabs(h), g) == fabs(h)) {
-        t = O::div(apq, h);
+        t = RO::div(apq, h);
     } else {
-        const T theta = O::div(O::mul(T(0.5), h), apq);
-        t = O::div(T(1), O::add(fabs(theta), O::sqrt_(O::add(T(1), O::mul(theta, theta)))));
+        const T theta = RO::div(O::mul(T(0.5), h), apq);
+        t = RO::div(T(1), O::add(fabs(theta), RO::sqrt1p(O::mul(theta, theta))));
         if (theta < T(0)) t = -t;
     }
-    const T c = O::div(T(1), O::sqrt_(O::add(T(1), O::mul(t, t))));
+    const T c = RO::inv_sqrt1p(O::mul(t, t));
     const T s = O::mul(t, c);
-    const T tau = O::div(s, O::add(T(1), c));
+    const T tau = RO::div(s, O::add(T(1), c));
     a[P][P] = O::sub(a[P][P], O::mul(t, apq));
     a[Q][Q] = O::add(a[Q][Q], O::mul(t, apq));
     a[P][Q] = a[Q][P] = T(0);
@@ -94,9 +114,10 @@ __device__ __forceinline__ int jacobi3(T (&a)[3][3], T (&v)[3][3]) {
         }
         ++sweeps;
         const bool late = sweep > 4;
-        jacobi_rotate<0, 1, T, VEC>(a, v, late);
-        jacobi_rotate<0, 2, T, VEC>(a, v, late);
-        jacobi_rotate<1, 2, T, VEC>(a, v, late);
+        constexpr bool kFast = !EXACT && sizeof(T) == sizeof(float);
+        jacobi_rotate<0, 1, T, VEC, kFast>(a, v, late);
+        jacobi_rotate<0, 2, T, VEC, kFast>(a, v, late);
+        jacobi_rotate<1, 2, T, VEC, kFast>(a, v, late);
     }
     return sweeps;
 }
