@@ -1,4 +1,4 @@
-"""Serving (the Poisson request stream, scaled down): requests admitted while others run
+"""Serving (the Poisson request stream): requests admitted while others run
 overlap on the GPU, and every result equals the same request run alone."""
 
 import numpy as np
@@ -155,3 +155,47 @@ def test_native_server_resident_clouds(cuda, pgeof):
     assert sum(1 for r in reqs if r.cloud) >= 10
     for res in results:
         np.testing.assert_array_equal(res.features, expect[res.rid])
+
+
+def test_native_stream_at_the_serving_rate(cuda, pgeof):
+    """The serving workload's shape at its full rate for 4 s: Poisson arrivals
+    at 200 req/s, clouds log-uniform in [1,000, 500,000] points, k in
+    {16, 32, 64}, the four selected features, 8 slots and a 40 GB budget. Every
+    request completes, requests overlap on the GPU, and a sample of 40 results
+    equals the same requests run alone."""
+    import time
+
+    from point_geometric_features_gb300.serving import NativeServer, Request, poisson_arrivals, radius_for_count
+
+    pool = _pool(24, 1_000, 500_000, seed=13)
+    feats = [pgeof.Verticality, pgeof.Curvature, pgeof.Planarity, pgeof.Normal_z]
+    rng = np.random.default_rng(14)
+    times = poisson_arrivals(200.0, 4.0, 15)
+    reqs = []
+    for i, _ in enumerate(times):
+        xyz = pool[int(rng.integers(len(pool)))]
+        k = int(rng.choice([16, 32, 64]))
+        reqs.append(Request(i, xyz, k, radius_for_count(xyz, 1.5 * k), feats))
+    server = NativeServer(slots=8, budget_bytes=40 << 30)
+    try:
+        t0 = time.perf_counter()
+        for req, t in zip(reqs, times):
+            now = time.perf_counter() - t0
+            if t > now:
+                time.sleep(t - now)
+            req.arrival = t0 + t
+            server.submit(req)
+        results = server.drain(len(reqs))
+        peak = server.adm.peak_in_flight
+    finally:
+        server.close()
+    assert len(reqs) > 600 and len(results) == len(reqs)
+    assert peak > 1
+    lat = np.array([r.latency_ms for r in results])
+    print(f"[serving] {len(reqs)} requests, p50 {np.percentile(lat, 50):.3f} ms, p99 {np.percentile(lat, 99):.3f} ms, "
+          f"peak in flight {peak}")
+    by_rid = {r.rid: r for r in results}
+    for rid in np.random.default_rng(16).choice(len(reqs), 40, replace=False):
+        r = reqs[int(rid)]
+        np.testing.assert_array_equal(by_rid[int(rid)].features,
+                                      pgeof.compute_features_selected(r.xyz, r.radius, r.max_knn, feats))
