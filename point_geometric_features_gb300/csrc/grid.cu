@@ -222,8 +222,12 @@ struct EdgeKey {
     }
 };
 std::mutex g_edge_mu;
-EdgeKey g_edge_keys[16];
-double g_edge_vals[16];
+// 256 entries: a request server cycles through many clouds (the serving
+// stream draws from ~100), and a miss costs two trial histograms with their
+// host round trips.
+constexpr int kEdgeCache = 256;
+EdgeKey g_edge_keys[kEdgeCache];
+double g_edge_vals[kEdgeCache];
 int g_edge_n = 0, g_edge_next = 0;
 
 bool edge_cache_get(const EdgeKey& k, double& h) {
@@ -245,8 +249,8 @@ void edge_cache_put(const EdgeKey& k, double h) {
         }
     g_edge_keys[g_edge_next] = k;
     g_edge_vals[g_edge_next] = h;
-    g_edge_next = (g_edge_next + 1) % 16;
-    g_edge_n = std::min(g_edge_n + 1, 16);
+    g_edge_next = (g_edge_next + 1) % kEdgeCache;
+    g_edge_n = std::min(g_edge_n + 1, kEdgeCache);
 }
 
 // Grid dimensions for edge h (x edge h / xsub), or false when it would
