@@ -242,6 +242,7 @@ struct BatchWorkspace {
     uint32_t* nn_ptr = nullptr;
     uint32_t* words = nullptr;
     uint32_t* scan_part = nullptr;
+    unsigned long long* defer = nullptr;  // the feature pass's exact-solve queue
 };
 
 namespace {
@@ -271,6 +272,7 @@ size_t layout(BatchWorkspace& w, char* base) {
     w.nn_ptr = (uint32_t*)take((n + 1) * 4);
     w.words = (uint32_t*)take((n + 8) * 4);
     w.scan_part = (uint32_t*)take((cells / 1024 + 2) * 4);
+    w.defer = (unsigned long long*)take((n + 1) * 8);
     return o;
 }
 
@@ -362,7 +364,7 @@ int run_pipeline(BatchWorkspace& w, const float* xyz, uint32_t* idx, float* d2, 
         uniform_ptr_kernel<<<blocks_for(n + 1, 256, di->sm_count), 256, 0, s>>>(w.nn_ptr, n, w.k);
         count_launch();
         PGEOF_TRY(launch_features(w.xyz4, n, idx, n * w.k, w.nn_ptr, n, true, 1, nullptr, 0, features, nullptr, s,
-                                  w.off, nc));
+                                  w.off, nc, nullptr, 0, 0, false, w.defer));
     }
     return PGEOF_OK;
 }

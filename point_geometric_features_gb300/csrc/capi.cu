@@ -454,6 +454,14 @@ struct SmemLimit {
     int limit;
 };
 std::vector<SmemLimit> g_smem_limit;
+// Shared-memory carveout preference last set on each (device, kernel) (-1:
+// the driver's default).
+struct CarveEntry {
+    int device;
+    const void* kernel;
+    int carveout;
+};
+std::vector<CarveEntry> g_carve;
 
 // Cache of page-locked host blocks behind pgeof_host_alloc / pgeof_host_free.
 struct HostPool {
@@ -506,6 +514,28 @@ int pgeof::kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* 
     n = std::max(n, 1);
     g_occ.push_back(OccEntry{dev, kernel, threads, smem, n});
     *per_sm = n;
+    return PGEOF_OK;
+}
+
+int pgeof::cap_smem_carveout(const void* kernel, int threads, int smem) {
+    int per_sm = 0;
+    PGEOF_TRY(kernel_blocks_per_sm(kernel, threads, smem, &per_sm));
+    int dev = 0;
+    PGEOF_CUDA_TRY(cudaGetDevice(&dev));
+    // 1 KB of shared memory is reserved per resident block
+    const int want = (size_t)per_sm * ((size_t)smem + 1024) > (size_t)196 * 1024 ? 85 : -1;
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    CarveEntry* cur = nullptr;
+    for (CarveEntry& e : g_carve)
+        if (e.device == dev && e.kernel == kernel) cur = &e;
+    if (!cur) {
+        g_carve.push_back(CarveEntry{dev, kernel, -1});
+        cur = &g_carve.back();
+    }
+    if (cur->carveout != want) {
+        PGEOF_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, want));
+        cur->carveout = want;
+    }
     return PGEOF_OK;
 }
 

@@ -79,6 +79,13 @@ int current_device_info(const DeviceInfo** out);
 // memory limit first when smem > 48 KB. Cached per (device, kernel, threads,
 // smem), so repeated launches pay no host-side query.
 int kernel_blocks_per_sm(const void* kernel, int threads, int smem, int* per_sm);
+// Keeps at least 60 KB of each SM's L1 as data cache for `kernel` at this
+// launch size: when its resident blocks would fill more than 196 KB of shared
+// memory the carveout preference is capped there (fewer resident blocks),
+// otherwise the driver's default stands. Random-gather kernels need the data
+// cache: every gather in flight holds an L1 sector until it returns, so with
+// the 228 KB carveout (28 KB of L1) their throughput halves.
+int cap_smem_carveout(const void* kernel, int threads, int smem);
 
 // ----------------------------------------------------------------- scratch
 // Stream-ordered scratch allocations from a library-owned memory pool that

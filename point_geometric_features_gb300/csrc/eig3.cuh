@@ -238,7 +238,10 @@ __device__ __forceinline__ float rayleigh(const Cov<float>& c, float x, float y,
 }
 
 // Float covariance -> PCA. `resolved` reports a re-solve in double.
-__device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, Pca<float>& out, bool& resolved) {
+// Float solve alone: returns false, with `out` unset, for a neighbourhood whose
+// relative eigen-gap is below kGapResolve (its eigenvectors need the exact
+// solve), so that callers can run that rare solve outside their hot loop.
+__device__ __forceinline__ bool pca_solve_f32_fast(const Cov<float>& cov, int order, Pca<float>& out) {
     float a[3][3], v[3][3], w[3];
     load_cov(cov, a);
     const int sweeps = jacobi3<float, true, false>(a, v);
@@ -248,19 +251,20 @@ __device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, 
     sort_ascending(w, v);
     const float gap = fminf(w[1] - w[0], w[2] - w[1]);
     const float scale = fmaxf(fabsf(w[0]), fabsf(w[2]));
-    resolved = false;
-    if (sweeps > 0 && gap < kGapResolve * scale) {
-        // ill-conditioned eigenvectors: exact solve of the same float matrix
-        resolved = true;
-        pca_solve_f64<float>(cov, order, &out);
-        return;
-    }
+    if (sweeps > 0 && gap < kGapResolve * scale) return false;
     if (sweeps > 0) {
         // eigenvalues to ~1e-14 |A| from the well-conditioned eigenvectors
 #pragma unroll
         for (int i = 0; i < 3; ++i) w[i] = rayleigh(cov, v[0][i], v[1][i], v[2][i]);
     }
     finish_pca<float, float>(w, v, order, out);
+    return true;
+}
+
+__device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, Pca<float>& out, bool& resolved) {
+    resolved = !pca_solve_f32_fast(cov, order, out);
+    // ill-conditioned eigenvectors: exact solve of the same float matrix
+    if (resolved) pca_solve_f64<float>(cov, order, &out);
 }
 
 // Eigenvalues only, float (for eigentropy scans). Approximate rotations are fine

@@ -54,7 +54,43 @@ struct FeatArgs {
     uint32_t row_base;             // this launch covers rows [row_base, row_base + n_points)
     int row_map_input;             // with row_map: row r also reads CSR row row_map[r].idx
     uint32_t slab_words;           // SLAB kernel: index words per warp in shared memory
+    // neighbourhoods left to the exact solve: defer[0] counts them, defer[1 ..]
+    // holds their output blocks (row * out_scales + scale), whose first six
+    // floats carry the covariance until features_exact_kernel replaces them
+    unsigned long long* defer;
+    uint64_t defer_cap;
 };
+
+// Float solve and features of one neighbourhood into f[0..10]; a neighbourhood
+// that needs the exact solve gets its covariance in f[0..5] and its output
+// block queued for features_exact_kernel. EXACT_INLINE runs the exact solve in
+// place instead (callers without a queue).
+template <bool EXACT_INLINE>
+__device__ __forceinline__ void solve_or_defer(const FeatArgs& a, const Cov<float>& c, uint64_t block, float (&f)[11],
+                                               uint32_t& flags) {
+    Pca<float> p;
+    if constexpr (EXACT_INLINE) {
+        bool res;
+        pca_solve_f32(c, a.order, p, res);
+        features11(p, f);
+        return;
+    }
+    if (pca_solve_f32_fast(c, a.order, p)) {
+        features11(p, f);
+        return;
+    }
+    f[0] = c.xx;
+    f[1] = c.xy;
+    f[2] = c.xz;
+    f[3] = c.yy;
+    f[4] = c.yz;
+    f[5] = c.zz;
+#pragma unroll
+    for (int q = 6; q < 11; ++q) f[q] = 0.0f;
+    const unsigned long long slot = atomicAdd(a.defer, 1ull);
+    if (slot < a.defer_cap) a.defer[1 + slot] = block;
+    else flags |= ERR_INTERNAL;
+}
 
 struct RowCloud {
     const float4* xyz4;
@@ -117,7 +153,15 @@ __device__ __forceinline__ void gather_row_slab(const uint32_t* idx, uint32_t co
 // coalesced loads, and both sweeps take them from there -- instead of each
 // thread reading its own row's indices from global memory in both sweeps.
 // Rows outside the slab (too long, out of order) read global memory.
-template <int S, bool MULTI, bool SLAB = false>
+//
+// EXACT_INLINE: neighbourhoods that need the exact solve get it in place.
+// Otherwise they are queued for features_exact_kernel, which keeps the rare
+// float64 solve (and the stack frame its call needs) out of this kernel: on
+// the 1M-point scene the k = 50 single-scale kernel drops from 76 to 44
+// registers and from 0.449 to 0.387 ms, and the queued solves then take one
+// float64 solve's latency (~0.06 ms) in features_exact_kernel -- about even
+// overall, with the hot kernel free of the float64 code.
+template <int S, bool MULTI, bool SLAB = false, bool EXACT_INLINE = false>
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
     extern __shared__ __align__(16) float smem_f[];
     float* stage = smem_f;  // kFeatThreads * n_scales * 11, then SLAB: a.slab_words per warp
@@ -127,7 +171,6 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
     for (int f = 0; f < row_w; ++f) stage[f * kFeatThreads + tid] = 0.0f;  // column-major staging
 
     uint32_t flags = 0;
-    unsigned n_resolved = 0;
     const bool row_ok = i < a.row_base + a.n_points;
     uint64_t b = 0, e = 0;
     if (row_ok) {
@@ -191,6 +234,11 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                 kmax = ks[s] > kmax ? ks[s] : kmax;
             }
         }
+        // output block of scale s of this row
+        const auto out_block = [&](int s) -> uint64_t {
+            const uint64_t dst = a.row_map ? (uint64_t)a.row_map[i].idx : (uint64_t)i;
+            return dst * (uint64_t)a.out_scales + (uint64_t)(a.scale_offset + s);
+        };
         if (n_active > 0) {
             // neighbours [j0, j1) of the row in order, indices from the slab or global memory
             const auto sweep = [&](uint32_t j0, uint32_t j1, auto&& f) {
@@ -263,12 +311,8 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                 c.yy = FDIV(cyy[0], kk);
                 c.yz = FDIV(cyz[0], kk);
                 c.zz = FDIV(czz[0], kk);
-                Pca<float> p;
-                bool res;
-                pca_solve_f32(c, a.order, p, res);
-                n_resolved += res;
                 float f[11];
-                features11(p, f);
+                solve_or_defer<EXACT_INLINE>(a, c, out_block(0), f, flags);
 #pragma unroll
                 for (int q = 0; q < 11; ++q) stage[q * kFeatThreads + tid] = f[q];
             } else {
@@ -297,12 +341,8 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
                     c.yy = st[3 * kFeatThreads];
                     c.yz = st[4 * kFeatThreads];
                     c.zz = st[5 * kFeatThreads];
-                    Pca<float> p;
-                    bool res;
-                    pca_solve_f32(c, a.order, p, res);
-                    n_resolved += res;
                     float f[11];
-                    features11(p, f);
+                    solve_or_defer<EXACT_INLINE>(a, c, out_block(s), f, flags);
 #pragma unroll
                     for (int q = 0; q < 11; ++q) st[q * kFeatThreads] = f[q];
                 }
@@ -310,7 +350,6 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
         }
     }
     if (flags) atomicOr(a.err, flags);
-    if (a.resolved && n_resolved) atomicAdd(a.resolved, (unsigned long long)n_resolved);
     __syncthreads();
     // coalesced write-out of the block's rows
     const uint32_t row0 = a.row_base + blockIdx.x * kFeatThreads;
@@ -355,6 +394,29 @@ __global__ void first_nb_kernel(const float* __restrict__ xyz, uint64_t n_xyz, c
         out[3 * i] = xyz[3 * id];
         out[3 * i + 1] = xyz[3 * id + 1];
         out[3 * i + 2] = xyz[3 * id + 2];
+    }
+}
+
+// The exact (float64) solve of the neighbourhoods features_kernel queued: each
+// queued output block holds its float covariance in its first six floats and
+// gets its 11 features in their place.
+__global__ void __launch_bounds__(128) features_exact_kernel(float* __restrict__ out,
+                                                             const unsigned long long* __restrict__ defer,
+                                                             uint64_t cap, int order, unsigned long long* resolved) {
+    const uint64_t n = min((uint64_t)defer[0], cap);
+    if (resolved && blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(resolved, (unsigned long long)n);
+    // one solve per thread: a solve is a long dependent chain of float64
+    // operations (~60 us on the 1M-point scene whatever the grid), so the
+    // kernel's time is one solve's latency
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+        float* o = out + defer[1 + t] * 11;
+        const Cov<float> c{o[0], o[1], o[2], o[3], o[4], o[5]};
+        Pca<float> p;
+        pca_solve_f64<float>(c, order, &p);
+        float f[11];
+        features11(p, f);
+#pragma unroll
+        for (int q = 0; q < 11; ++q) o[q] = f[q];
     }
 }
 
@@ -638,28 +700,49 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
     const size_t stage_bytes = (size_t)kFeatThreads * a.n_scales * 11 * sizeof(float);
     const unsigned blocks = ceil_div_u(a.n_points, kFeatThreads);
     KernelTimer kt("features_kernel", s);
-    if (a.slab_words > 0) {
-        const size_t smem = stage_bytes + (size_t)(kFeatThreads / 32) * a.slab_words * sizeof(uint32_t);
-        auto kern = a.n_clouds > 0 ? features_kernel<S, true, true> : features_kernel<S, false, true>;
-        int per_sm = 0;
-        PGEOF_TRY(kernel_blocks_per_sm((const void*)kern, kFeatThreads, (int)smem, &per_sm));
-        kern<<<blocks, kFeatThreads, smem, s>>>(a);
-    } else if (a.n_clouds > 0) {
-        features_kernel<S, true><<<blocks, kFeatThreads, stage_bytes, s>>>(a);
-    } else {
-        features_kernel<S, false><<<blocks, kFeatThreads, stage_bytes, s>>>(a);
-    }
+    const bool slab = a.slab_words > 0;
+    using Kern = void (*)(const FeatArgs);
+    const Kern kern = slab ? (a.n_clouds > 0 ? features_kernel<S, true, true> : features_kernel<S, false, true>)
+                           : (a.n_clouds > 0 ? features_kernel<S, true> : features_kernel<S, false>);
+    const size_t smem = stage_bytes + (slab ? (size_t)(kFeatThreads / 32) * a.slab_words * sizeof(uint32_t) : 0);
+    PGEOF_TRY(cap_smem_carveout((const void*)kern, kFeatThreads, (int)smem));
+    kern<<<blocks, kFeatThreads, smem, s>>>(a);
     count_launch();
     return check_launch("features_kernel");
 }
+
+static int launch_features_exact(float* out, const unsigned long long* defer, uint64_t cap,
+                                 unsigned long long* resolved, cudaStream_t s) {
+    const DeviceInfo* di;
+    PGEOF_TRY(current_device_info(&di));
+    const unsigned blocks = (unsigned)std::min<uint64_t>(ceil_div_u(cap, 128), (uint64_t)di->sm_count * 2);
+    KernelTimer kt("features_exact_kernel", s);
+    features_exact_kernel<<<blocks, 128, 0, s>>>(out, defer, cap, eig_order(), resolved);
+    count_launch();
+    return check_launch("features_exact_kernel");
+}
+
+static int launch_features_impl(FeatArgs& a, uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales,
+                                int n_scales, uint64_t nnz, uint32_t uniform_k, cudaStream_t s);
 
 int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint64_t nnz, const uint32_t* ptr,
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off,
                     int n_clouds, const SPoint<float>* row_map, uint32_t uniform_k, uint64_t row_base,
-                    bool row_map_input) {
+                    bool row_map_input, unsigned long long* defer) {
     if (n_points == 0) return PGEOF_OK;
+    if (!full && n_scales <= 0) return PGEOF_OK;
+    // queue for the exact solves: a count and one slot per output block
+    const uint64_t cap = n_points * (uint64_t)(full ? 1 : n_scales);
+    Scratch own;
+    if (!defer) {
+        PGEOF_TRY(own.alloc((cap + 1) * sizeof(unsigned long long), s));
+        defer = own.as<unsigned long long>();
+    }
+    PGEOF_CUDA_TRY(cudaMemsetAsync(defer, 0, sizeof(unsigned long long), s));
     FeatArgs a{};
+    a.defer = defer;
+    a.defer_cap = cap;
     a.row_map = row_map;
     a.row_map_input = row_map && row_map_input ? 1 : 0;
     a.uniform_k = uniform_k;
@@ -676,19 +759,26 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
     a.err = device_error_word();
     a.resolved = resolved;
     a.out = out;
+    PGEOF_TRY(launch_features_impl(a, n_points, full, k_min, scales, n_scales, nnz, uniform_k, s));
+    return launch_features_exact(out, defer, cap, resolved, s);
+}
+
+static int launch_features_impl(FeatArgs& a, uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales,
+                                int n_scales, uint64_t nnz, uint32_t uniform_k, cudaStream_t s) {
     if (full) {
         a.full = 1;
         a.k_min = (uint32_t)std::min<uint64_t>(k_min, 0xffffffffull);
         a.n_scales = 1;
         a.out_scales = 1;
         a.scale_offset = 0;
-        // Index slab sized for uniform rows exactly, CSR rows up to 64 neighbours
-        // on average (longer warps read global memory). Single-scale passes
-        // only: on the 1M-point scene the slab takes the k = 50 compute_features
-        // pass from 0.485 to 0.454 ms, but the 3-scale pass (whose output
-        // staging already holds 33 floats per row) from 0.706 to 0.917 ms.
-        const uint32_t ks = uniform_k ? uniform_k : 64u;
-        a.slab_words = use_index_slab() && !a.row_map_input && ks <= 128 ? 32u * ks + 4u : 0u;
+        // Index slab sized for the average row (warps whose rows run longer
+        // read global memory). Single-scale passes only: on the 1M-point scene
+        // it takes the k = 50 compute_features pass from 0.437 to 0.388 ms and
+        // k = 20 from 0.172 to 0.171 ms, but the 3-scale pass from 0.607 to
+        // 0.613 ms. A larger slab than the rows need costs resident blocks
+        // (k = 50 rows in a 64-neighbour slab: 0.399 ms).
+        const uint64_t ks = uniform_k ? uniform_k : (nnz + n_points - 1) / n_points;
+        a.slab_words = use_index_slab() && !a.row_map_input && ks >= 1 && ks <= 128 ? 32u * (uint32_t)ks + 4u : 0u;
         return launch_features_s<1>(a, s);
     }
     a.full = 0;
@@ -877,7 +967,7 @@ extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xy
     a.err = err;
     a.resolved = nullptr;
     const size_t smem = (size_t)kFeatThreads * 11 * sizeof(float);
-    features_kernel<1, false><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
+    features_kernel<1, false, false, true><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
     count_launch();
     return check_launch("features_kernel (noalloc)");
 }

@@ -21,7 +21,7 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
                     uint64_t n_points, bool full, uint64_t k_min, const uint32_t* scales, int n_scales,
                     float* out, unsigned long long* resolved, cudaStream_t s, const uint64_t* cloud_off = nullptr,
                     int n_clouds = 0, const SPoint<float>* row_map = nullptr, uint32_t uniform_k = 0,
-                    uint64_t row_base = 0, bool row_map_input = false);
+                    uint64_t row_base = 0, bool row_map_input = false, unsigned long long* defer = nullptr);
 // The three CSR feature passes for a float64 cloud (kind 0 compute_features,
 // 1 multiscale over the HOST array `scales`, 2 optimal); out is float64 with
 // rows of 11, n_scales * 11 or 12 values.
