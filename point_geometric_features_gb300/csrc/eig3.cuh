@@ -107,7 +107,7 @@ __device__ __forceinline__ int jacobi3(T (&a)[3][3], T (&v)[3][3]) {
     const int max_sweeps = EXACT ? 64 : 16;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         if (a[0][1] == T(0) && a[0][2] == T(0) && a[1][2] == T(0)) break;
-        if (!EXACT) {
+        if constexpr (!EXACT) {
             const T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
             const T scale = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
             if (sweep >= 2 && off <= T(1e-9) * scale) break;
@@ -219,6 +219,69 @@ __device__ __forceinline__ DFloat df_mul(DFloat x, float a) {
     return quick_two_sum(p.hi, __fmaf_rn(x.lo, a, p.lo));
 }
 
+// ---- a double-float number type for the eigen solver: the same Jacobi
+// iteration as the float64 solver, on the FP32 pipes. Addition is the
+// accurate double-float sum (both halves' errors carried), products use the
+// fused multiply-add for the exact error of hi * hi, division and square root
+// take one correction step from the float quotient / root (Dekker 1971;
+// Knuth TAOCP vol. 2, 4.2.2; Bailey's double-double arithmetic). Relative
+// precision ~2^-44 down to magnitudes of ~1e-30.
+struct DF {
+    float hi, lo;
+    DF() = default;
+    __device__ __forceinline__ DF(float h) : hi(h), lo(0.0f) {}
+    __device__ __forceinline__ DF(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit operator float() const { return __fadd_rn(hi, lo); }
+};
+__device__ __forceinline__ DF df_norm(float h, float l) {
+    const DFloat q = quick_two_sum(h, l);
+    return DF(q.hi, q.lo);
+}
+__device__ __forceinline__ DF operator-(DF x) { return DF(-x.hi, -x.lo); }
+__device__ __forceinline__ bool operator==(DF x, DF y) { return x.hi == y.hi && x.lo == y.lo; }
+__device__ __forceinline__ bool operator<(DF x, DF y) { return x.hi < y.hi || (x.hi == y.hi && x.lo < y.lo); }
+using ::fabs;  // the float and double overloads stay visible beside DF's
+__device__ __forceinline__ DF fabs(DF x) { return x.hi < 0.0f || (x.hi == 0.0f && x.lo < 0.0f) ? -x : x; }
+__device__ __forceinline__ DF df_sum(DF x, DF y) {
+    const DFloat s = two_sum(x.hi, y.hi);
+    const DFloat t = two_sum(x.lo, y.lo);
+    DF r = df_norm(s.hi, __fadd_rn(s.lo, t.hi));
+    return df_norm(r.hi, __fadd_rn(r.lo, t.lo));
+}
+__device__ __forceinline__ DF df_prod(DF x, DF y) {
+    const DFloat p = two_prod(x.hi, y.hi);
+    return df_norm(p.hi, __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.lo, p.lo)));
+}
+__device__ __forceinline__ DF df_quot(DF x, DF y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    DF r = df_sum(x, -df_prod(y, DF(q1)));
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    r = df_sum(r, -df_prod(y, DF(q2)));
+    const float q3 = __fdiv_rn(r.hi, y.hi);
+    return df_sum(df_norm(q1, q2), DF(q3));
+}
+__device__ __forceinline__ DF df_root(DF x) {
+    if (!(x.hi > 0.0f)) return DF(0.0f);
+    const float r = __fsqrt_rn(x.hi);
+    const DFloat r2 = two_prod(r, r);
+    const DF e = df_sum(x, -DF(r2.hi, r2.lo));
+    return df_norm(r, __fdiv_rn(e.hi, __fmul_rn(2.0f, r)));
+}
+
+}  // namespace pgeof
+
+template <>
+struct XOps<pgeof::DF> {
+    using D = pgeof::DF;
+    static __device__ __forceinline__ D add(D a, D b) { return pgeof::df_sum(a, b); }
+    static __device__ __forceinline__ D sub(D a, D b) { return pgeof::df_sum(a, -b); }
+    static __device__ __forceinline__ D mul(D a, D b) { return pgeof::df_prod(a, b); }
+    static __device__ __forceinline__ D div(D a, D b) { return pgeof::df_quot(a, b); }
+    static __device__ __forceinline__ D sqrt_(D a) { return pgeof::df_root(a); }
+};
+
+namespace pgeof {
+
 // Rayleigh quotient v^T A v / v^T v of the float covariance, evaluated in
 // double-float. With v accurate to angle t the result is within t^2 * gap of
 // the exact eigenvalue, and rounding contributes ~2^-46 |A| instead of the
@@ -261,10 +324,98 @@ __device__ __forceinline__ bool pca_solve_f32_fast(const Cov<float>& cov, int or
     return true;
 }
 
+
+// 1 / sqrt(1 + x) in double-float: the float reciprocal root and one Newton
+// step (r + r (1 - y r^2) / 2).
+__device__ __forceinline__ DF df_rsqrt1p(DF x) {
+    const DF y = df_sum(DF(1.0f), x);
+    const float r = rsqrtf(y.hi);
+    const DFloat r2 = two_prod(r, r);
+    const DF e = df_sum(DF(1.0f), -df_prod(y, DF(r2.hi, r2.lo)));
+    return df_norm(r, __fmul_rn(__fmul_rn(0.5f, r), e.hi));
+}
+
+// One Jacobi rotation in double-float annihilating a[P][Q]:
+// t = sgn(d) 2 a_pq / (|d| + sqrt(d^2 + 4 a_pq^2)) with d = a_qq - a_pp (the
+// smaller root of t^2 + 2 theta t - 1, theta = d / (2 a_pq)), c = 1/sqrt(1 + t^2),
+// s = t c; one division and two roots per rotation.
+template <int P, int Q>
+__device__ __forceinline__ void df_rotate(DF (&a)[3][3], DF (&v)[3][3]) {
+    constexpr int R = 3 - P - Q;
+    const DF apq = a[P][Q];
+    if (apq.hi == 0.0f) return;
+    const DF d = df_sum(a[Q][Q], -a[P][P]);
+    const DF two_apq(__fmul_rn(2.0f, apq.hi), __fmul_rn(2.0f, apq.lo));
+    const DF root = df_root(df_sum(df_prod(d, d), df_prod(two_apq, two_apq)));
+    DF t = df_quot(two_apq, df_sum(fabs(d), root));
+    if (d.hi < 0.0f) t = -t;
+    const DF c = df_rsqrt1p(df_prod(t, t));
+    const DF sn = df_prod(t, c);
+    const DF tap = df_prod(t, apq);
+    a[P][P] = df_sum(a[P][P], -tap);
+    a[Q][Q] = df_sum(a[Q][Q], tap);
+    a[P][Q] = a[Q][P] = DF(0.0f);
+    const DF arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = df_sum(df_prod(c, arp), -df_prod(sn, arq));
+    a[R][Q] = a[Q][R] = df_sum(df_prod(sn, arp), df_prod(c, arq));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const DF vkp = v[k][P], vkq = v[k][Q];
+        v[k][P] = df_sum(df_prod(c, vkp), -df_prod(sn, vkq));
+        v[k][Q] = df_sum(df_prod(sn, vkp), df_prod(c, vkq));
+    }
+}
+
+// Relative eigen-gap below which the double-float solve is not trusted with
+// the eigenvectors (their error is ~2^-44 / gap) and the float64 solve runs.
+constexpr float kGapFloat64 = 1e-7f;
+
+// The exact solve of a small-gap neighbourhood: cyclic Jacobi in double-float
+// on the float covariance, swept until the off-diagonal is below 1e-15 of the
+// diagonal, whose eigenpairs agree with the float64 solver's to ~1e-7 for
+// relative gaps down to kGapFloat64; below that (exactly or nearly degenerate
+// neighbourhoods) the float64 solver itself. A float64 solve is one long
+// chain of slow dependent operations on this GPU (~60 us); the double-float
+// one runs on the FP32 pipes. Returns false when the float64 solve ran.
+__device__ __forceinline__ bool pca_solve_refined(const Cov<float>& cov, int order, Pca<float>& out) {
+    DF a[3][3], v[3][3], w[3];
+    a[0][0] = DF(cov.xx);
+    a[0][1] = a[1][0] = DF(cov.xy);
+    a[0][2] = a[2][0] = DF(cov.xz);
+    a[1][1] = DF(cov.yy);
+    a[1][2] = a[2][1] = DF(cov.yz);
+    a[2][2] = DF(cov.zz);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = DF(i == j ? 1.0f : 0.0f);
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        const float off = fabsf(a[0][1].hi) + fabsf(a[0][2].hi) + fabsf(a[1][2].hi);
+        const float diag = fabsf(a[0][0].hi) + fabsf(a[1][1].hi) + fabsf(a[2][2].hi);
+        if (!(off > 1e-15f * diag)) break;
+        df_rotate<0, 1>(a, v);
+        df_rotate<0, 2>(a, v);
+        df_rotate<1, 2>(a, v);
+    }
+    w[0] = a[0][0];
+    w[1] = a[1][1];
+    w[2] = a[2][2];
+    sort_ascending(w, v);
+    const float gap = fminf((float)df_sum(w[1], -w[0]), (float)df_sum(w[2], -w[1]));
+    const float scale = fmaxf(fabsf((float)w[0]), fabsf((float)w[2]));
+    if (!(gap >= kGapFloat64 * scale) || !(scale > 0.0f)) {
+        pca_solve_f64<float>(cov, order, &out);
+        return false;
+    }
+    finish_pca<float, DF>(w, v, order, out);
+    return true;
+}
+
+// Float solve; ill-conditioned eigenvectors get the exact solve of the same
+// float matrix in place (`resolved`).
 __device__ __forceinline__ void pca_solve_f32(const Cov<float>& cov, int order, Pca<float>& out, bool& resolved) {
     resolved = !pca_solve_f32_fast(cov, order, out);
-    // ill-conditioned eigenvectors: exact solve of the same float matrix
-    if (resolved) pca_solve_f64<float>(cov, order, &out);
+    if (resolved) pca_solve_refined(cov, order, out);
 }
 
 // Eigenvalues only, float (for eigentropy scans). Approximate rotations are fine

@@ -156,11 +156,10 @@ __device__ __forceinline__ void gather_row_slab(const uint32_t* idx, uint32_t co
 //
 // EXACT_INLINE: neighbourhoods that need the exact solve get it in place.
 // Otherwise they are queued for features_exact_kernel, which keeps the rare
-// float64 solve (and the stack frame its call needs) out of this kernel: on
-// the 1M-point scene the k = 50 single-scale kernel drops from 76 to 44
-// registers and from 0.449 to 0.387 ms, and the queued solves then take one
-// float64 solve's latency (~0.06 ms) in features_exact_kernel -- about even
-// overall, with the hot kernel free of the float64 code.
+// exact solve (and the stack frame its call needs) out of this kernel: on the
+// 1M-point scene the k = 50 single-scale kernel drops from 76 to 44 registers
+// and from 0.449 to 0.387 ms, and the few hundred queued solves take one
+// double-float solve's latency (~0.016 ms) in features_exact_kernel.
 template <int S, bool MULTI, bool SLAB = false, bool EXACT_INLINE = false>
 __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
     extern __shared__ __align__(16) float smem_f[];
@@ -405,14 +404,12 @@ __global__ void __launch_bounds__(128) features_exact_kernel(float* __restrict__
                                                              uint64_t cap, int order, unsigned long long* resolved) {
     const uint64_t n = min((uint64_t)defer[0], cap);
     if (resolved && blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(resolved, (unsigned long long)n);
-    // one solve per thread: a solve is a long dependent chain of float64
-    // operations (~60 us on the 1M-point scene whatever the grid), so the
-    // kernel's time is one solve's latency
+    // one solve per thread: the kernel's time is one solve's latency
     for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
         float* o = out + defer[1 + t] * 11;
         const Cov<float> c{o[0], o[1], o[2], o[3], o[4], o[5]};
         Pca<float> p;
-        pca_solve_f64<float>(c, order, &p);
+        pca_solve_refined(c, order, p);
         float f[11];
         features11(p, f);
 #pragma unroll

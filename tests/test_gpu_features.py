@@ -158,6 +158,36 @@ def test_degenerate_neighbourhoods(cuda, pgeof):
     _assert_features(f, ref, "degenerate neighbourhoods")
 
 
+def test_near_degenerate_neighbourhoods(cuda, pgeof):
+    """Neighbourhoods whose two largest or two smallest eigenvalues differ by a
+    relative 1e-2 ... 1e-7 (regular polygons and octahedra, stretched by 1 + eps
+    and rotated): the eigenvectors there are ill-conditioned, which is where
+    the small-gap solves (double-float, float64 below 1e-7) take over."""
+    rng = np.random.default_rng(23)
+    blocks = []
+    for eps in (1e-2, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7, 0.0):
+        for _ in range(40):
+            m = int(rng.integers(8, 40))
+            a = np.linspace(0.0, 2.0 * np.pi, m, endpoint=False) + rng.random()
+            if rng.random() < 0.5:  # polygon: two equal large eigenvalues, small normal one
+                p = np.stack([np.cos(a) * (1.0 + eps), np.sin(a), 1e-3 * rng.standard_normal(m)], 1)
+            else:  # polygon plus poles: the two small eigenvalues nearly equal
+                p = np.stack([np.cos(a), np.sin(a), np.zeros(m)], 1) * np.array([0.2, 0.2 * (1.0 + eps), 0.0])
+                p[:, 0] += np.linspace(-1.0, 1.0, m)
+            q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+            blocks.append(p @ q.T * rng.uniform(0.1, 10.0) + rng.uniform(-50.0, 50.0, 3))
+    xyz = np.concatenate(blocks).astype(np.float32)
+    sizes = [len(b) for b in blocks]
+    nn = np.arange(xyz.shape[0], dtype=np.uint32)
+    nn_ptr = np.r_[0, np.cumsum(sizes)].astype(np.uint32)
+    f = pgeof.compute_features(xyz, nn, nn_ptr)
+    ref = oracle.compute_features(xyz, nn, nn_ptr)
+    _assert_features(f, ref, "near-degenerate neighbourhoods")
+    f3 = pgeof.compute_features_multiscale(xyz, nn, nn_ptr, [4, 8])
+    ref3 = oracle.compute_features_multiscale(xyz, nn, nn_ptr, [4, 8])
+    _assert_features(f3, ref3, "near-degenerate neighbourhoods, scales 4 and 8")
+
+
 def test_csr_validation(cuda, pgeof):
     xyz = uniform_cube(100, seed=1)
     nn = np.arange(100, dtype=np.uint32)
