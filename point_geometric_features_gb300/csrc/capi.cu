@@ -904,6 +904,12 @@ int pgeof_compute_features_selected_f64(const double* xyz, int64_t n, double sea
 }
 
 // ---------------------------------------------------------------- host API
+// First row of chunk c of a C-chunk host pipeline over m rows (equal chunks:
+// a half-size first chunk, so that the first transfer starts earlier,
+// measured slower on the 1M-point scene -- kNN 3.07 -> 3.21 ms, multiscale
+// 1.61 -> 1.74 ms).
+static uint64_t pipeline_row(uint64_t m, int c, int C) { return m * (uint64_t)c / (uint64_t)C; }
+
 int pgeof_host_knn_search_f32(const float* data, int64_t n_data, const float* query, int64_t n_query,
                               uint32_t knn, uint32_t* indices, float* sqr_dist) {
     PGEOF_TRY(check_cloud(n_data, "data"));
@@ -945,7 +951,7 @@ int pgeof_host_knn_search_f32(const float* data, int64_t n_data, const float* qu
     if (cudaEventRecord(ev[0], s) != cudaSuccess || cudaStreamWaitEvent(cout, ev[0], 0) != cudaSuccess)
         status = fail(PGEOF_ERR_CUDA, "knn pipeline: stream ordering failed");
     for (int c = 0; c < C && status == PGEOF_OK; ++c) {
-        const uint64_t r0 = m * c / C, r1 = m * (c + 1) / C;
+        const uint64_t r0 = pipeline_row(m, c, C), r1 = pipeline_row(m, c + 1, C);
         if (r1 == r0) continue;
         SPoint<float>* qs = nullptr;
         status = sort_queries<float>(qbase + 3 * r0, r1 - r0, grid.g, qmem, &qs, qstart_mem, s);
@@ -1023,7 +1029,9 @@ static int host_features(const float* xyz, int64_t n_xyz, const uint32_t* nn, in
     PGEOF_TRY(xyz4.alloc(std::max<uint64_t>(n_xyz, 1) * sizeof(float4), s));
     PGEOF_TRY(pad_xyz(d_xyz.as<float>(), n_xyz, xyz4.as<float4>(), s));
     const cudaStream_t cin = host_copy_stream(0), cout = host_copy_stream(1);
-    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, nn_bytes / (24ull << 20)));
+    // ~48 MB of neighbour lists per chunk (1M-point k=50 multiscale through
+    // the numpy API: 4 chunks 1.61 ms, 8 chunks 1.78 ms, 16 chunks 1.69 ms)
+    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, nn_bytes / (48ull << 20)));
     std::vector<cudaEvent_t> ev(2 * C + 3, nullptr);  // start, (upload, kernel) per chunk, 2 final
     for (auto& e : ev) PGEOF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     int status = PGEOF_OK;
@@ -1036,7 +1044,7 @@ static int host_features(const float* xyz, int64_t n_xyz, const uint32_t* nn, in
             break;
         }
         for (int c = 0; c < C && status == PGEOF_OK; ++c) {
-            const uint64_t r0 = n * c / C, r1 = n * (c + 1) / C;
+            const uint64_t r0 = pipeline_row(n, c, C), r1 = pipeline_row(n, c + 1, C);
             if (r1 == r0) continue;
             const uint64_t lo = std::min<uint64_t>(nn_ptr[r0], total);
             const uint64_t hi = std::min<uint64_t>(std::max<uint64_t>(nn_ptr[r1], lo), total);
