@@ -6,10 +6,13 @@
 // diagonalised by cyclic Jacobi rotations (Golub & Van Loan, "Matrix
 // Computations", sec. 8.5) in float. Jacobi is backward stable, so the float
 // eigenvectors are accurate to ~eps*|A|/gap; when the smallest eigen-gap is
-// below kGapResolve*|A| the same float covariance is diagonalised again in
-// double with exactly the arithmetic of the CPU oracle's solver (explicit
-// round-to-nearest ops, no FMA), so ill-conditioned neighbourhoods reproduce
-// the exact solution of the float covariance instead of float noise. Eigenpairs
+// below kGapResolve*|A| the same float covariance is diagonalised again
+// exactly: by Jacobi in double-float arithmetic (pca_solve_refined), and for
+// relative gaps below kGapFloat64 -- where the eigenvectors are fixed only by
+// the sequence of rotations -- in double with exactly the arithmetic of the
+// CPU oracle's solver (explicit round-to-nearest ops, no FMA), so
+// ill-conditioned neighbourhoods reproduce the exact solution of the float
+// covariance instead of float noise. Eigenpairs
 // are then ordered as Eigen's SelfAdjointEigenSolver returns them (ascending;
 // for equal values the first minimum stays first), because the reference feeds
 // them to the formulas unsorted (pca.hpp:79-97).

@@ -12,7 +12,9 @@
 // the prefix produces -- the second keeps one product accumulator set per
 // scale; the scales' covariances then wait in shared memory and one copy of
 // the eigen solver handles them in turn. Output rows are staged in shared
-// memory and leave the block as one coalesced slab.
+// memory and leave the block as one coalesced slab. The few neighbourhoods
+// whose float eigenvectors are ill-conditioned are queued and solved exactly
+// afterwards by features_exact_kernel.
 #include <algorithm>
 #include <atomic>
 #include <mutex>
