@@ -1029,9 +1029,10 @@ static int host_features(const float* xyz, int64_t n_xyz, const uint32_t* nn, in
     PGEOF_TRY(xyz4.alloc(std::max<uint64_t>(n_xyz, 1) * sizeof(float4), s));
     PGEOF_TRY(pad_xyz(d_xyz.as<float>(), n_xyz, xyz4.as<float4>(), s));
     const cudaStream_t cin = host_copy_stream(0), cout = host_copy_stream(1);
-    // ~48 MB of neighbour lists per chunk (1M-point k=50 multiscale through
-    // the numpy API: 4 chunks 1.61 ms, 8 chunks 1.78 ms, 16 chunks 1.69 ms)
-    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, nn_bytes / (48ull << 20)));
+    // ~24 MB of neighbour lists per chunk (1M-point k=50 multiscale through
+    // the numpy API, repeated runs: 8 chunks 1.74-1.75 ms, 4 chunks 1.85-1.87
+    // ms; single runs of 2 / 12 / 16 chunks 1.83 / 1.68 / 1.69 ms)
+    const int C = (int)std::min<uint64_t>(8, std::max<uint64_t>(2, nn_bytes / (24ull << 20)));
     std::vector<cudaEvent_t> ev(2 * C + 3, nullptr);  // start, (upload, kernel) per chunk, 2 final
     for (auto& e : ev) PGEOF_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     int status = PGEOF_OK;

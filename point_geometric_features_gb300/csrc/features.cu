@@ -163,7 +163,7 @@ __device__ __forceinline__ void gather_row_slab(const uint32_t* idx, uint32_t co
 // and from 0.449 to 0.387 ms, and the few hundred queued solves take one
 // double-float solve's latency (~0.016 ms) in features_exact_kernel.
 template <int S, bool MULTI, bool SLAB = false, bool EXACT_INLINE = false>
-__global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
+__device__ __forceinline__ void features_body(const FeatArgs& a) {
     extern __shared__ __align__(16) float smem_f[];
     float* stage = smem_f;  // kFeatThreads * n_scales * 11, then SLAB: a.slab_words per warp
     const int tid = threadIdx.x;
@@ -378,6 +378,21 @@ __global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_con
         }
     }
 }
+
+template <int S, bool MULTI, bool SLAB = false, bool EXACT_INLINE = false>
+__global__ void __launch_bounds__(kFeatThreads) features_kernel(const __grid_constant__ FeatArgs a) {
+    features_body<S, MULTI, SLAB, EXACT_INLINE>(a);
+}
+
+// The 3-scale pass (compute_features_multiscale with three scales, the
+// 1M-point benchmark's case) compiled for 8 resident blocks per SM: 64
+// registers and a 44-byte spill instead of 76 registers and 6 blocks (0.607 ->
+// 0.591 ms on the 1M-point scene).
+template <bool MULTI>
+__global__ void __launch_bounds__(kFeatThreads, 8) features3_kernel(const __grid_constant__ FeatArgs a) {
+    features_body<3, MULTI, false, false>(a);
+}
+
 
 // Coordinates of each CSR row's first neighbour (point 0's for an empty or
 // invalid row): the key by which rows are ordered in space.
@@ -701,8 +716,11 @@ static int launch_features_s(const FeatArgs& a, cudaStream_t s) {
     KernelTimer kt("features_kernel", s);
     const bool slab = a.slab_words > 0;
     using Kern = void (*)(const FeatArgs);
-    const Kern kern = slab ? (a.n_clouds > 0 ? features_kernel<S, true, true> : features_kernel<S, false, true>)
-                           : (a.n_clouds > 0 ? features_kernel<S, true> : features_kernel<S, false>);
+    Kern kern = slab ? (a.n_clouds > 0 ? features_kernel<S, true, true> : features_kernel<S, false, true>)
+                     : (a.n_clouds > 0 ? features_kernel<S, true> : features_kernel<S, false>);
+    if constexpr (S == 3) {
+        if (!slab) kern = a.n_clouds > 0 ? features3_kernel<true> : features3_kernel<false>;
+    }
     const size_t smem = stage_bytes + (slab ? (size_t)(kFeatThreads / 32) * a.slab_words * sizeof(uint32_t) : 0);
     PGEOF_TRY(cap_smem_carveout((const void*)kern, kFeatThreads, (int)smem));
     kern<<<blocks, kFeatThreads, smem, s>>>(a);
