@@ -158,7 +158,10 @@ __device__ __forceinline__ float axis_gap(float v, int c, float o, float h, floa
 
 // Visit every point of the cells in `bx` (rows clipped to the sphere of radius
 // Rf around q when prune). All lanes call visit(valid, d2, idx) together.
-template <typename T, typename F>
+// U > 1 loads U batches of 32 points before visiting them (U loads in flight
+// per lane: for the few, large queries of the list passes, whose warps
+// otherwise wait on one load at a time).
+template <typename T, typename F, int U = 1>
 __device__ __forceinline__ void visit_box(const GridView<T>& gv, uint32_t* run_start, uint32_t* run_len,
                                           const T (&q)[3], const Box& bx, bool prune, float Rf, F&& visit) {
     const GridParams& g = gv.g;
@@ -215,6 +218,37 @@ __device__ __forceinline__ void visit_box(const GridView<T>& gv, uint32_t* run_s
         const uint32_t excl = incl - c_len;
         const uint32_t total = __shfl_sync(FULL, incl, 31);
         int r_base = 0;
+        if constexpr (U > 1) {
+            for (uint32_t base0 = 0; base0 < total; base0 += 32 * U) {
+                SPoint<T> p[U];
+                bool valid[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const uint32_t base = base0 + 32u * u;
+                    const uint32_t bit =
+                        (lane < nrows && excl > base && excl < base + 32) ? (1u << (excl - base)) : 0u;
+                    const uint32_t M = __reduce_or_sync(FULL, bit);
+                    const int r = r_base + __popc(M & (0xffffffffu >> (31 - lane)));
+                    const uint32_t pos = base + lane;
+                    valid[u] = pos < total;
+                    const uint32_t r_st = __shfl_sync(FULL, c_st, r);
+                    const uint32_t r_ex = __shfl_sync(FULL, excl, r);
+                    if (valid[u]) p[u] = gv.pts[r_st + (pos - r_ex)];
+                    r_base = __popc(__ballot_sync(FULL, lane < nrows && excl <= base + 32)) - 1;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    T d2 = T(0);
+                    uint32_t idx = 0;
+                    if (valid[u]) {
+                        d2 = dist2<T>(q, p[u]);
+                        idx = p[u].idx;
+                    }
+                    visit(valid[u], d2, idx);
+                }
+            }
+            continue;
+        }
         for (uint32_t base = 0; base < total; base += 32) {
             const uint32_t bit = (lane < nrows && excl > base && excl < base + 32) ? (1u << (excl - base)) : 0u;
             const uint32_t M = __reduce_or_sync(FULL, bit);
@@ -258,7 +292,7 @@ __device__ __forceinline__ void query_cell(const GridParams& g, float x, float y
 // Pilot bound on the k-th neighbour distance: grow a block of cells around
 // the query until it holds >= k points (cell counts only), then a 32-bin
 // histogram of the block's squared distances gives tau^2 >= d_k^2.
-template <typename T>
+template <typename T, int U = 1>
 __device__ __forceinline__ T pilot_tau2(const GridView<T>& gv, uint32_t* hist32, uint32_t* run_start,
                                         uint32_t* run_len, const T (&q)[3], uint32_t k) {
     const GridParams& g = gv.g;
@@ -299,14 +333,15 @@ __device__ __forceinline__ T pilot_tau2(const GridView<T>& gv, uint32_t* hist32,
     hist32[lane] = 0;
     __syncwarp();
     T dmax = T(0);
-    visit_box<T>(gv, run_start, run_len, q, bx, false, 0.0f, [&](bool valid, T d2, uint32_t) {
+    const auto hist = [&](bool valid, T d2, uint32_t) {
         if (valid) {
             const float x = (float)d2 * sb;
             const int bin = x >= 31.0f ? 31 : (int)x;
             atomicAdd(&hist32[bin], 1u);
             dmax = max(dmax, d2);
         }
-    });
+    };
+    visit_box<T, decltype(hist)&, U>(gv, run_start, run_len, q, bx, false, 0.0f, hist);
     __syncwarp();
     dmax = warp_max(dmax);
     uint32_t incl = hist32[lane];
@@ -960,7 +995,7 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
                         const float t = bound * 1.00002f + 1e-30f + g.margin * 1e-3f;  // rounding slack
                         tau2 = t * t;
                     } else {
-                        tau2 = pilot_tau2<float>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
+                        tau2 = pilot_tau2<float, LIST ? 4 : 1>(gv, ws->hist, ws->run_start, ws->run_len, q, k);
                     }
                 } else {
                     strict = true;
@@ -974,18 +1009,19 @@ __device__ __forceinline__ void fast_search_body(const FastArgs& a) {
                 ws->hist[lane] = 0;
                 ws->hist[lane + 32] = 0;
                 __syncwarp();
-                visit_box<float>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
-                                 [&](bool valid, float d2, uint32_t idx) {
-                                     const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
-                                     const uint32_t mask = __ballot_sync(FULL, take);
-                                     if (take) {
-                                         const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
-                                         if (pos < a.cap) keys[pos] = make_key(d2, idx);
-                                         const float x = d2 * sb;
-                                         atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
-                                     }
-                                     count += __popc(mask);
-                                 });
+                const auto collect = [&](bool valid, float d2, uint32_t idx) {
+                    const bool take = valid && (strict ? (d2 < tau2) : (d2 <= tau2));
+                    const uint32_t mask = __ballot_sync(FULL, take);
+                    if (take) {
+                        const uint32_t pos = count + __popc(mask & ((1u << lane) - 1u));
+                        if (pos < a.cap) keys[pos] = make_key(d2, idx);
+                        const float x = d2 * sb;
+                        atomicAdd(&ws->hist[x >= (float)(kSelBins - 1) ? kSelBins - 1 : (int)x], 1u);
+                    }
+                    count += __popc(mask);
+                };
+                visit_box<float, decltype(collect)&, LIST ? 4 : 1>(gv, ws->run_start, ws->run_len, q, rb, true, tf,
+                                                                   collect);
                 __syncwarp();
                 const bool short_knn = a.mode == MODE_KNN && count < k;  // the optimistic radius fell short
                 const uint32_t n_sel = a.mode == MODE_KNN ? k : min(count, k);
