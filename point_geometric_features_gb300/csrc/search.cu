@@ -160,7 +160,8 @@ __device__ __forceinline__ float axis_gap(float v, int c, float o, float h, floa
 // Rf around q when prune). All lanes call visit(valid, d2, idx) together.
 // U > 1 loads U batches of 32 points before visiting them (U loads in flight
 // per lane: for the few, large queries of the list passes, whose warps
-// otherwise wait on one load at a time).
+// otherwise wait on one load at a time; 1M-point scene, k = 50: both list
+// passes 0.131 ms with U = 1, 0.110 ms with U = 4, 0.113 ms with U = 8).
 template <typename T, typename F, int U = 1>
 __device__ __forceinline__ void visit_box(const GridView<T>& gv, uint32_t* run_start, uint32_t* run_len,
                                           const T (&q)[3], const Box& bx, bool prune, float Rf, F&& visit) {
