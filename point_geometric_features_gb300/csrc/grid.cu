@@ -113,17 +113,23 @@ __global__ void scan_partials_kernel(const uint32_t* __restrict__ in, uint32_t G
     }
 }
 
-// Single block: exclusive scan of the tile partials in place.
+// Single block: exclusive scan of the tile partials in place, four
+// consecutive partials per thread (1024 per block step).
 __global__ void scan_top_kernel(uint32_t* partial, uint32_t nb) {
     __shared__ uint32_t carry;
     __shared__ uint32_t warp_sums[kScanThreads / 32];
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (uint32_t base = 0; base < nb; base += kScanThreads) {
-        const uint32_t i = base + threadIdx.x;
-        const uint32_t v = i < nb ? partial[i] : 0u;
-        uint32_t x = v;
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < nb; base += 4 * kScanThreads) {
+        uint32_t v[4], s = 0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t i = base + threadIdx.x * 4 + q;
+            v[q] = i < nb ? partial[i] : 0u;
+            s += v[q];
+        }
+        uint32_t x = s;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
@@ -132,10 +138,16 @@ __global__ void scan_top_kernel(uint32_t* partial, uint32_t nb) {
         __syncthreads();
         uint32_t wo = 0;
         for (int q = 0; q < w; ++q) wo += warp_sums[q];
-        const uint32_t incl = x + wo + carry;
-        if (i < nb) partial[i] = incl - v;
+        uint32_t run = carry + wo + x - s;
+        const uint32_t block_end = carry + wo + x;  // thread kScanThreads - 1: the step's total
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t i = base + threadIdx.x * 4 + q;
+            if (i < nb) partial[i] = run;
+            run += v[q];
+        }
         __syncthreads();
-        if (threadIdx.x == kScanThreads - 1) carry = incl;
+        if (threadIdx.x == kScanThreads - 1) carry = block_end;
         __syncthreads();
     }
 }
