@@ -46,7 +46,6 @@ struct FeatArgs {
     int order;
     float* out;
     uint32_t* err;
-    unsigned long long* resolved;  // neighbourhoods re-solved in double (stats)
     // multi-cloud batches: row r belongs to the cloud c with off[c] <= r < off[c+1];
     // its neighbour indices are local to that cloud's slice of xyz4
     const uint64_t* cloud_off;
@@ -774,7 +773,6 @@ int launch_features(const float4* xyz4, uint64_t n_xyz, const uint32_t* nn, uint
     a.n_points = (uint32_t)n_points;
     a.order = eig_order();
     a.err = device_error_word();
-    a.resolved = resolved;
     a.out = out;
     PGEOF_TRY(launch_features_impl(a, n_points, full, k_min, scales, n_scales, nnz, uniform_k, s));
     return launch_features_exact(out, defer, cap, resolved, s);
@@ -982,7 +980,6 @@ extern "C" int pgeof_compute_features_f32_noalloc(const float* xyz, int64_t n_xy
     a.order = eig_order();
     a.out = features;
     a.err = err;
-    a.resolved = nullptr;
     const size_t smem = (size_t)kFeatThreads * 11 * sizeof(float);
     features_kernel<1, false, false, true><<<ceil_div_u((uint64_t)n_points, kFeatThreads), kFeatThreads, smem, s>>>(a);
     count_launch();
